@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""bench.py — throughput of the GB300 PSD projection on the n = 8192 workload.
+
+Workload (one "step" = one auto-scaled projection of one matrix):
+  n = 8192, A = Q diag(lambda) Q^T with Q from the QR of a seeded N(0, 1)
+  matrix and lambda ~ U[-1, 1] (seeded), symmetrised and stored in FP32, passed
+  as the FP64 column-major matrix the reference's API takes.  The exact
+  projection Q diag(max(lambda, 0)) Q^T is the FP64 oracle every result's
+  relative Frobenius error is quoted against.
+
+Arms:
+  (default)          this library: composite_FP32_auto_scale through the C ABI
+                     (Lanczos bound + 10-step filter on fp16x3 tensor-core
+                     products + fused ReLU reconstruction), inputs resident in
+                     HBM (one 537 MB input per step, more than L2, no flush);
+                     `e2e` runs psdgb_project_host("composite_FP32") on pinned
+                     host buffers with both copies inside the timed region.
+  --impl reference   the reference's CPU path named by the goal: FP64 LAPACK
+                     dsyevd EVD projection (eig_FP64_psd's math) on all host
+                     cores, on a bounded n = 4096 sample scaled by n^3; plus
+                     a replay of the reference's own cuBLAS call sequence for
+                     composite_FP32_auto_scale (plain FP32 Sgemm) on the GPU.
+
+Multi-GPU: a single projection does not shard, so N GPUs run N independent
+replicas (one process per GPU under torchrun) and `value` is N x steps over
+the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "n=8192 proj/s & TC TFLOP/s vs plain FP32 at equal error; p50/p99 serve latency"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=8192)
+    ap.add_argument("--precision", default="fp16x3")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side-by-side", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=4096)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas)
+# ---------------------------------------------------------------------------
+
+def dist_setup():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_workload(n: int, seed: int = 0):
+    """X (FP64 device, FP32-representable values) and its exact projection."""
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    G = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+    Q, _ = torch.linalg.qr(G)
+    del G
+    g.manual_seed(seed + 1)
+    lam = torch.rand(n, generator=g, dtype=torch.float64, device="cuda") * 2.0 - 1.0
+    A = (Q * lam) @ Q.T
+    A = 0.5 * (A + A.T)
+    X = A.float().double()                       # "stored in FP32"
+    del A
+    P = (Q * lam.clamp(min=0.0)) @ Q.T
+    P = 0.5 * (P + P.T)
+    del Q
+    torch.cuda.synchronize()
+    return X.contiguous(), P.contiguous(), float((lam < 0).double().mean())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        if self.path and os.path.exists(self.path):
+            for line in Path(self.path).read_text().splitlines():
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+            os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+
+        def num(s):
+            try:
+                return float(s)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        smax = [num(r[1]) for r in rows if num(r[1]) is not None]
+        loaded = [v for v in sm if smax and v >= 0.5 * max(smax)] or sm
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, val in zip(names, r[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        power = [num(r[2]) for r in rows if num(r[2]) is not None]
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "power_w_max": max(power) if power else None, "samples": len(rows)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"bf16_tflops": d.get("bf16_tflops"), "bf16_tflops_sustained": d.get("bf16_tflops_sustained"),
+                "hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def dense_equiv_flops(n: int, steps: int) -> float:
+    """(3K + 1) 2 n^3: the reference's GEMM chain as full GEMMs."""
+    return (3 * steps + 1) * 2.0 * float(n) ** 3
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: FP64 LAPACK dsyevd projection (eig_FP64_psd's math)
+# ---------------------------------------------------------------------------
+
+def cpu_evd_projection_rate(X, n_full: int, n_sample: int, repeats: int = 1):
+    import numpy as np
+
+    from oracle import reference_port as rp
+
+    xs = X[:n_sample, :n_sample].cpu().numpy()
+    xs = 0.5 * (xs + xs.T)
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        rp.eig_psd(xs)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    scale = (n_full / n_sample) ** 3
+    return 1.0 / (t * scale), t, scale
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_ours(args, rank, world):
+    import torch
+
+    import psd_projection_gb300 as psd
+
+    n, K, W = args.n, args.steps, args.warmup
+    prec = psd.PRECISIONS[args.precision]
+    sched = psd.SCHEDULE_FP16 if args.precision == "fp16" else psd.SCHEDULE_FP32
+    X, P, neg_frac = make_workload(n, seed=0)
+    # One resident input per step: every step reads a fresh 537 MB matrix (> L2).
+    inputs = [torch.empty_like(X) for _ in range(W + K)]
+    stream = torch.cuda.current_stream()
+
+    def refill():
+        for t in inputs:
+            t.copy_(X)
+        torch.cuda.synchronize()
+
+    refill()
+    for i in range(W):
+        psd.composite(inputs[i], prec, sched, auto_scale=True)
+    torch.cuda.synchronize()
+
+    lib = psd._capi.lib()
+    lib.psdgb_product_timing_read(None, None, None, 1)
+    lib.psdgb_product_timing_enable(1)
+    launches0 = psd.kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        barrier(world)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for i in range(K):
+            psd.composite(inputs[W + i], prec, sched, auto_scale=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    lib.psdgb_product_timing_enable(0)
+    launches = psd.kernel_launch_count() - launches0
+    ms_total = e0.elapsed_time(e1)
+    ms_total = max_over_ranks(ms_total, world)
+    import ctypes
+
+    pms, pl, pfl = ctypes.c_double(), ctypes.c_uint64(), ctypes.c_double()
+    lib.psdgb_product_timing_read(ctypes.byref(pms), ctypes.byref(pl), ctypes.byref(pfl), 1)
+    err = psd.rel_frobenius(inputs[W + K - 1], P)
+    clocks = clk.summary()
+
+    value = world * K / (ms_total / 1e3)
+    steps_filter = 7 if sched == psd.SCHEDULE_FP16 else 10
+    tc = {
+        "dense_equiv_tflops": value / world * dense_equiv_flops(n, steps_filter) / 1e12,
+        "executed_mma_tflops": (pfl.value / max(pl.value, 1)) / (pms.value / max(pl.value, 1) / 1e3) / 1e12
+        if pl.value else None,
+    }
+    peaks = measured_peaks()
+    per_launch_flops = pfl.value / max(pl.value, 1)
+    per_launch_ms = pms.value / max(pl.value, 1)
+    achieved = per_launch_flops / (per_launch_ms / 1e3) / 1e12 if pl.value else None
+    peak = peaks["bf16_tflops_sustained"]
+    roofline = {
+        "bound": "tensor", "kernel": "tc_sym_kernel (symmetric product, fp16x3 split operands)",
+        "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "frac": (achieved / peak) if achieved else None,
+        "peak_source": f"{peaks['source']} bf16_tflops_sustained (of {peaks['source']})",
+        "flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms, "launches": pl.value,
+        "share_of_step": (pms.value / ms_total) if ms_total else None,
+        "traffic": None,
+    }
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "proj/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic: A = Q diag(lambda) Q^T, Q = QR(N(0,1)) seed 0, "
+                                          "lambda ~ U[-1,1] seed 1, stored FP32, passed as FP64",
+        "config": {"workload": f"single dense projection n={n} (lambda uniform in [-1,1]), "
+                               "composite_FP32_auto_scale", "n": n, "precision": args.precision,
+                   "lanczos_steps": 20, "filter_steps": steps_filter,
+                   "l2": "each step projects its own resident input (8n^2 B > L2); no flush",
+                   "negative_fraction": neg_frac, "rel_frobenius_err": err, "replicas": world},
+        "tc_tflops": tc, "gpu_launches": launches, "clocks": clocks, "roofline": roofline,
+    }
+    if rank != 0:
+        return None
+
+    # e2e: the C-ABI host-buffer call, both copies inside the timed region.
+    Xh = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    Xh.copy_(X.cpu())
+    Oh = torch.empty_like(Xh)
+    psd.project_host("composite_FP32", Xh, Oh)  # warm
+    Ke = max(2, min(K, 5))
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        psd.project_host("composite_FP32", Xh, Oh)
+    te = time.perf_counter() - t0
+    out["e2e"] = {"value": Ke / te, "unit": "proj/s", "h2d_bytes_per_step": 8 * n * n,
+                  "d2h_bytes_per_step": 8 * n * n, "api": "psdgb_project_host(\"composite_FP32\")",
+                  "rel_frobenius_err": psd.rel_frobenius(Oh.cuda(), P)}
+
+    if not args.no_side_by_side:
+        side = {}
+        for name, steps in (("fp16", 3), ("bf16x9", 3), ("bf16x6", 3), ("bf16x3", 3), ("fp32_simt", 1)):
+            p = psd.PRECISIONS[name]
+            s = psd.SCHEDULE_FP16 if name == "fp16" else psd.SCHEDULE_FP32
+            t = inputs[0]
+            t.copy_(X)
+            psd.composite(t, p, s, auto_scale=True)
+            for j in range(steps):
+                inputs[1 + j].copy_(X)
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record()
+            for j in range(steps):
+                psd.composite(inputs[1 + j], p, s, auto_scale=True)
+            ev1.record()
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1) / steps
+            side[name] = {"proj_s": 1e3 / ms, "ms": ms, "rel_frobenius_err": psd.rel_frobenius(inputs[steps], P),
+                          "method": {"fp16": "composite_FP16", "bf16x9": "composite_FP32_emulated",
+                                     "fp32_simt": "plain FP32 (CUDA cores)"}.get(name, name)}
+        out["side_by_side"] = side
+
+    if world == 1 and not args.no_cpu_baseline:
+        rate, t, scale = cpu_evd_projection_rate(X, n, args.cpu_sample_n)
+        out["cpu_baseline"] = {"value": rate, "unit": "proj/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"FP64 LAPACK dsyevd projection V max(L,0) V^T (scipy eigh 'evd') of "
+                                         f"the leading {args.cpu_sample_n}^2 block, {t:.2f} s, scaled by "
+                                         f"(n/{args.cpu_sample_n})^3 = {scale:g}"}
+    return out
+
+
+def run_reference(args, rank, world):
+    import torch
+
+    if rank != 0:
+        return None
+    n, K, W = args.n, args.steps, args.warmup
+    X, P, _ = make_workload(n, seed=0)
+    # CPU path: FP64 dsyevd projection on all host cores, bounded sample, scaled by n^3.
+    for _ in range(W):
+        cpu_evd_projection_rate(X, n, args.cpu_sample_n)
+    t0 = time.perf_counter()
+    rates = []
+    for _ in range(K):
+        r, _, scale = cpu_evd_projection_rate(X, n, args.cpu_sample_n)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = statistics.median(rates)
+    out = {
+        "metric": METRIC, "value": value, "unit": "proj/s", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (same workload as the default arm)", "impl": "reference",
+        "config": {"workload": f"single dense projection n={n} (lambda uniform in [-1,1])", "n": n},
+        "cpu_baseline": {"value": value, "unit": "proj/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"FP64 LAPACK dsyevd projection of the leading {args.cpu_sample_n}^2 block per "
+                                   f"step, scaled by (n/{args.cpu_sample_n})^3 = {scale:g}; {K} steps in "
+                                   f"{wall:.1f} s"},
+        "e2e": {"value": value, "unit": "proj/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    # The reference's own GPU method (plain FP32 composite), replayed on cuBLAS.
+    try:
+        from oracle import gpu_replay
+
+        torch.backends.cuda.matmul.allow_tf32 = False
+        t = X.clone()
+        gpu_replay.composite_fp32_auto_scale_(t)
+        torch.cuda.synchronize()
+        reps = 2
+        ts = [X.clone() for _ in range(reps)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for t in ts:
+            gpu_replay.composite_fp32_auto_scale_(t)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        err = float(torch.linalg.matrix_norm(ts[-1] - P) / torch.linalg.matrix_norm(P))
+        out["gpu_fp32_composite_replay"] = {
+            "proj_s": 1e3 / ms, "ms": ms, "rel_frobenius_err": err,
+            "what": "composite_FP32_auto_scale call sequence (cuBLAS FP32 Sgemm, TF32 off; FP64 Dgemv Lanczos) "
+                    "replayed through torch on the GPU"}
+    except Exception as exc:  # noqa: BLE001 - report, do not fail the CPU arm
+        out["gpu_fp32_composite_replay"] = {"unavailable": repr(exc)[:200]}
+    return out
+
+
+def main():
+    args = parse_args()
+    rank, world = dist_setup()
+    res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * psdgb.h — C ABI of the GB300-native PSD-cone projection library (libpsdgb.so).
+ *
+ * Every entry point takes plain pointers and sizes.  Device matrices are n x n
+ * FP64, column-major, leading dimension n, exactly as the reference library's
+ * `double* mat` arguments.  The matrix is assumed symmetric; where it is not,
+ * the library uses the symmetric matrix defined by its upper triangle
+ * (row <= column), the same triangle cuSOLVER syevd reads in eig_FP64_psd.
+ *
+ * All calls are blocking on the given stream (they end with a stream
+ * synchronisation), like the reference functions, which end in
+ * cudaDeviceSynchronize.  Unlike the reference (whose CHECK_* macros print and
+ * continue, include/psd_projection/check.h:18-57), every call returns a status
+ * code; psdgb_last_error() gives the message of the last failure on the
+ * calling thread.
+ *
+ * Reference interfaces replaced (paths inside ComputationalRobotics/psd_projection):
+ *   psdgb_composite            composite_FP16 / composite_FP32 / composite_FP32_emulated
+ *                              (include/psd_projection/composite_FP16.h:12-18,
+ *                               composite_FP32.h:12-17, composite_FP32_emulated.h:17-22)
+ *   psdgb_composite_auto_scale composite_*_auto_scale
+ *                              (composite_FP16.h:26-33, composite_FP32.h:24-30,
+ *                               composite_FP32_emulated.h:29-35)
+ *   psdgb_two_norm             approximate_two_norm (include/psd_projection/lanczos.h:11-17)
+ *   psdgb_eig_psd              eig_FP64_psd / eig_FP32_psd
+ *                              (include/psd_projection/eig_FP64_psd.h:14-20, eig_FP32_psd.h:14-20)
+ *   psdgb_project              the MATLAB wrapper's method dispatch
+ *                              (MATLAB/psd_projection_MATLAB.cu:62-188), device buffers
+ *   psdgb_project_host         the same dispatch on host buffers, with the H2D/D2H copies
+ *                              of MATLAB/psd_projection_MATLAB.cu:104-106,171-173
+ */
+#ifndef PSDGB_H
+#define PSDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum psdgb_status {
+    PSDGB_OK = 0,
+    PSDGB_ERR_INVALID_ARGUMENT = 1, /* bad size, null pointer, unknown method/precision */
+    PSDGB_ERR_CUDA = 2,             /* a CUDA runtime call or a kernel launch failed */
+    PSDGB_ERR_OUT_OF_MEMORY = 3,    /* internal workspace could not be allocated */
+    PSDGB_ERR_UNSUPPORTED = 4,      /* device is not sm_103 (the kernels are sm_103a only) */
+    PSDGB_ERR_DEVICE_TIMEOUT = 5,   /* a bounded device-side wait gave up (error flag set) */
+    PSDGB_ERR_SOLVER = 6,           /* cuSOLVER reported a failure (eig_* entry points) */
+    PSDGB_ERR_WORKSPACE_TOO_SMALL = 7
+} psdgb_status;
+
+/* Operand arithmetic of the filter's matrix products.  Every mode accumulates
+ * in FP32; the elementwise polynomial combination is done in FP32. */
+typedef enum psdgb_precision {
+    PSDGB_PREC_FP32_SIMT = 0, /* plain FP32 FMA on the CUDA cores (the reference's Sgemm numerics) */
+    PSDGB_PREC_FP16 = 1,      /* one FP16 term per operand, tcgen05 kind::f16 */
+    PSDGB_PREC_BF16 = 2,      /* one BF16 term per operand */
+    PSDGB_PREC_FP16X3 = 3,    /* FP16 hi/lo split, products hi*hi + hi*lo + lo*hi */
+    PSDGB_PREC_BF16X3 = 4,    /* BF16 hi/lo split, 3 products */
+    PSDGB_PREC_BF16X6 = 5,    /* BF16 3-term split, the 6 products of order <= 2 */
+    PSDGB_PREC_BF16X9 = 6     /* BF16 3-term split, all 9 products (FP32 emulation) */
+} psdgb_precision;
+
+/* Polynomial schedule of the sign filter. */
+typedef enum psdgb_schedule {
+    PSDGB_SCHEDULE_FP32 = 0,  /* 10 quintic steps, safety factor 1.001 on the first 8
+                                 (src/composite_FP32.cu:73-99) */
+    PSDGB_SCHEDULE_FP16 = 1   /* 7 quintic steps, safety factor 1.01 on every step
+                                 (src/composite_FP16.cu:93-113) */
+} psdgb_schedule;
+
+/* Residual formula of the Lanczos upper bound. */
+typedef enum psdgb_residual {
+    PSDGB_RESIDUAL_REFERENCE = 0, /* r = A*y - theta*y, what src/lanczos.cu:246-260 computes
+                                     (its copy at :255 leaves ry = A*y) */
+    PSDGB_RESIDUAL_EXACT = 1      /* r = A^T*A*y - theta*y, the Ritz residual of A^T*A */
+} psdgb_residual;
+
+/* ---- library information ------------------------------------------------ */
+int psdgb_version(void);
+const char* psdgb_last_error(void);
+/* Host-side name of a precision/schedule enum value, or NULL. */
+const char* psdgb_precision_name(int precision);
+
+/* Per-step coefficients (a, b, c) of a filter schedule after the safety
+ * scaling p(x/s), as FP32 triples in out[3*i .. 3*i+2].  Writes at most cap
+ * triples and returns the number of steps, or -1 for an unknown schedule. */
+int psdgb_filter_coefficients(int schedule, float* out, int cap);
+
+/* ---- workspace -------------------------------------------------------------
+ * Bytes of device workspace psdgb_composite / psdgb_composite_auto_scale need
+ * for the filter operands of an n x n matrix at the given precision (three
+ * split matrices of Np x Np, Np = n rounded up to 128).  A caller that passes
+ * ws == NULL, or ws_bytes below this size, gets the library's own cached
+ * workspace (allocated on first use, grown on demand and kept until
+ * psdgb_release_workspace or process exit).  The Lanczos state (a few
+ * n-vectors and the n x max_iter basis) always comes from a cached buffer. */
+size_t psdgb_composite_workspace_size(int64_t n, int precision);
+psdgb_status psdgb_release_workspace(void);
+
+/* ---- the hot path ---------------------------------------------------------- */
+
+/* Composite polynomial filter on a matrix whose spectrum lies in [-1, 1]
+ * (composite_FP16 / composite_FP32 / composite_FP32_emulated).  In place. */
+psdgb_status psdgb_composite(int precision, int schedule, double* d_mat, int64_t n,
+                             void* d_ws, size_t ws_bytes, void* stream);
+
+/* Lanczos bound, scale by 1/up, filter, and rescale by up
+ * (composite_*_auto_scale).  max_iter = 20 and tol = 1e-10 are the
+ * reference's defaults (src/composite_FP32.cu:177-179 uses the defaults of
+ * lanczos.h:16).  seed selects the start vector.  up_out may be NULL. */
+psdgb_status psdgb_composite_auto_scale(int precision, int schedule, double* d_mat, int64_t n,
+                                        int64_t lanczos_max_iter, double lanczos_tol,
+                                        uint64_t seed, int residual_mode,
+                                        void* d_ws, size_t ws_bytes, void* stream,
+                                        double* up_out);
+
+/* Lanczos spectral-norm bound (approximate_two_norm): lo and up are host
+ * pointers.  The matrix is not modified. */
+psdgb_status psdgb_two_norm(const double* d_A, int64_t n, double* lo, double* up,
+                            int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                            void* d_ws, size_t ws_bytes, void* stream);
+
+/* Diagnostic variant of psdgb_two_norm: also returns the Lanczos coefficients
+ * (alpha, beta: host arrays of max_iter doubles, may be NULL), the number of
+ * completed iterations and the Ritz value theta. */
+psdgb_status psdgb_two_norm_ex(const double* d_A, int64_t n, double* lo, double* up,
+                               int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                               void* d_ws, size_t ws_bytes, void* stream,
+                               double* h_alpha, double* h_beta, int64_t* nb_iter,
+                               double* theta);
+
+/* EVD projection through cuSOLVER syevd (eig_FP64_psd when fp64 != 0, else
+ * eig_FP32_psd).  When d_eigs_out is not NULL it receives the n unclipped
+ * eigenvalues in ascending order (FP64, device), which the reference returns
+ * as a library-allocated pointer. */
+psdgb_status psdgb_eig_psd(int fp64, double* d_mat, int64_t n, double* d_eigs_out, void* stream);
+
+/* Method-string dispatch of the MATLAB wrapper: "composite_FP16",
+ * "composite_FP32", "composite_FP32_emulated", "eig_FP64", "eig_FP32".  The
+ * composite methods run the Lanczos bound with the reference defaults.  For
+ * eig_* methods d_eigs_out (n doubles, may be NULL) gets the eigenvalues. */
+psdgb_status psdgb_project(const char* method, double* d_mat, int64_t n, double* d_eigs_out,
+                           void* stream);
+
+/* psdgb_project on host buffers: copies h_in to the device, projects, and
+ * copies the result to h_out (h_out may equal h_in).  h_eigs_out (n doubles,
+ * host) may be NULL.  Pinned host buffers give the fastest copies. */
+psdgb_status psdgb_project_host(const char* method, const double* h_in, double* h_out,
+                                int64_t n, double* h_eigs_out, void* stream);
+
+/* ---- diagnostics ------------------------------------------------------------ */
+/* Product-kernel timing: when enabled, the library records a CUDA event pair
+ * on the caller's stream around every filter-product launch and adds the
+ * elapsed times up when the call synchronises.  psdgb_product_timing_read
+ * returns the accumulated milliseconds, launches and executed MMA flops
+ * (term products x 2 x 128 x 128 x K per tile) since the last reset. */
+psdgb_status psdgb_product_timing_enable(int on);
+psdgb_status psdgb_product_timing_read(double* ms, uint64_t* launches, double* mma_flops, int reset);
+
+/* Number of kernels this library launched on the calling process so far. */
+uint64_t psdgb_kernel_launch_count(void);
+/* Relative Frobenius error ||a - b||_F / ||b||_F of two n x n device FP64
+ * matrices, reduced in FP64 on the device. */
+psdgb_status psdgb_rel_frobenius(const double* d_a, const double* d_b, int64_t n, double* out,
+                                 void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSDGB_H */

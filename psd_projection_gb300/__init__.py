@@ -1,0 +1,240 @@
+"""psd_projection_gb300 — GB300-native PSD-cone projection (Python mirror of the C ABI).
+
+The functions here mirror the reference library's C++ entry points
+(ComputationalRobotics/psd_projection include/psd_projection/*.h) with the same
+names and argument meaning, on torch CUDA tensors:
+
+    composite_FP16(mat)                 composite_FP16_auto_scale(mat)
+    composite_FP32(mat)                 composite_FP32_auto_scale(mat)
+    composite_FP32_emulated(mat)        composite_FP32_emulated_auto_scale(mat)
+    approximate_two_norm(A, max_iter=20, tol=1e-10) -> (lo, up)
+    eig_FP64_psd(mat, return_eigenvalues=False)
+    eig_FP32_psd(mat, return_eigenvalues=False)
+    project(method, mat)                # the MATLAB wrapper's method strings
+    project_host(method, array)         # the same on host (numpy) buffers
+
+`mat` is an n x n float64 CUDA tensor projected in place.  Its memory is read
+as the reference reads `double* mat`: column-major.  A C-contiguous torch
+tensor M therefore stands for the column-major matrix M^T; for the symmetric
+matrices these functions take, the two are the same.  Where a matrix is not
+exactly symmetric, its upper triangle (row <= column in the column-major
+sense) defines it, as in cuSOLVER syevd with CUBLAS_FILL_MODE_UPPER.
+
+Error behaviour: the reference prints and continues; this mirror raises
+PsdgbError with the library's message.  Every call runs the CUDA kernels of
+libpsdgb.so — there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+from . import _capi
+from ._capi import (DEFAULT_SEED, PREC_BF16, PREC_BF16X3, PREC_BF16X6, PREC_BF16X9, PREC_FP16, PREC_FP16X3,
+                    PREC_FP32_SIMT, PRECISIONS, RESIDUAL_EXACT, RESIDUAL_REFERENCE, SCHEDULE_FP16, SCHEDULE_FP32,
+                    PsdgbError)
+
+__all__ = [
+    "composite", "composite_FP16", "composite_FP16_auto_scale", "composite_FP32", "composite_FP32_auto_scale",
+    "composite_FP32_emulated", "composite_FP32_emulated_auto_scale", "approximate_two_norm", "lanczos_details",
+    "eig_FP64_psd", "eig_FP32_psd", "project", "project_host", "workspace_size", "filter_coefficients",
+    "kernel_launch_count", "rel_frobenius", "PsdgbError", "PRECISIONS", "METHODS",
+]
+
+# MATLAB method string -> (precision, schedule), MATLAB/psd_projection_MATLAB.cu:112-166.
+METHODS = {
+    "composite_FP16": (PREC_FP16, SCHEDULE_FP16),
+    "composite_FP32": (PREC_FP16X3, SCHEDULE_FP32),
+    "composite_FP32_emulated": (PREC_BF16X9, SCHEDULE_FP32),
+    "eig_FP64": None,
+    "eig_FP32": None,
+}
+
+
+def _torch():
+    import torch  # deferred: the C ABI itself needs no torch
+    return torch
+
+
+def _stream_ptr(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+def _check_mat(mat, name="mat"):
+    torch = _torch()
+    if not isinstance(mat, torch.Tensor) or not mat.is_cuda:
+        raise TypeError(f"{name} must be a CUDA tensor")
+    if mat.dtype != torch.float64:
+        raise TypeError(f"{name} must be float64 (the reference's double* mat)")
+    if mat.dim() != 2 or mat.shape[0] != mat.shape[1]:
+        raise ValueError(f"{name} must be square, got {tuple(mat.shape)}")
+    if not mat.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    return mat.shape[0]
+
+
+def _ws_args(workspace):
+    if workspace is None:
+        return None, 0
+    return ctypes.c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+
+
+def workspace_size(n: int, precision: int = PREC_FP16X3) -> int:
+    """Device bytes of filter workspace for an n x n matrix at a precision."""
+    return int(_capi.lib().psdgb_composite_workspace_size(n, precision))
+
+
+def filter_coefficients(schedule: int = SCHEDULE_FP32) -> list[tuple[float, float, float]]:
+    """The (a, b, c) of every filter step after the safety scaling, as FP32."""
+    buf = (ctypes.c_float * 64)()
+    k = _capi.lib().psdgb_filter_coefficients(schedule, buf, 21)
+    if k < 0:
+        raise ValueError("unknown schedule")
+    return [(buf[3 * i], buf[3 * i + 1], buf[3 * i + 2]) for i in range(k)]
+
+
+def composite(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, auto_scale: bool = True,
+              max_iter: int = 20, tol: float = 1e-10, seed: int = DEFAULT_SEED,
+              residual: int = RESIDUAL_REFERENCE, workspace=None, stream=None) -> float:
+    """Project mat in place with the composite filter; returns the scale used (up, or 1)."""
+    n = _check_mat(mat)
+    ws, wsb = _ws_args(workspace)
+    lib = _capi.lib()
+    if auto_scale:
+        up = ctypes.c_double(1.0)
+        st = lib.psdgb_composite_auto_scale(precision, schedule, ctypes.c_void_p(mat.data_ptr()), n, max_iter, tol,
+                                            seed, residual, ws, wsb, _stream_ptr(stream), ctypes.byref(up))
+        _capi.check(st, "psdgb_composite_auto_scale")
+        return up.value
+    st = lib.psdgb_composite(precision, schedule, ctypes.c_void_p(mat.data_ptr()), n, ws, wsb, _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite")
+    return 1.0
+
+
+def composite_FP16(mat, workspace=None):
+    """composite_FP16 (include/psd_projection/composite_FP16.h:12-18): spectrum must lie in [-1, 1]."""
+    composite(mat, PREC_FP16, SCHEDULE_FP16, auto_scale=False, workspace=workspace)
+
+
+def composite_FP16_auto_scale(mat, workspace=None):
+    composite(mat, PREC_FP16, SCHEDULE_FP16, auto_scale=True, workspace=workspace)
+
+
+def composite_FP32(mat, workspace=None):
+    """composite_FP32 (include/psd_projection/composite_FP32.h:12-17): spectrum must lie in [-1, 1]."""
+    composite(mat, PREC_FP16X3, SCHEDULE_FP32, auto_scale=False, workspace=workspace)
+
+
+def composite_FP32_auto_scale(mat, workspace=None):
+    composite(mat, PREC_FP16X3, SCHEDULE_FP32, auto_scale=True, workspace=workspace)
+
+
+def composite_FP32_emulated(mat, workspace=None):
+    composite(mat, PREC_BF16X9, SCHEDULE_FP32, auto_scale=False, workspace=workspace)
+
+
+def composite_FP32_emulated_auto_scale(mat, workspace=None):
+    composite(mat, PREC_BF16X9, SCHEDULE_FP32, auto_scale=True, workspace=workspace)
+
+
+def lanczos_details(A, max_iter: int = 20, tol: float = 1e-10, seed: int = DEFAULT_SEED,
+                    residual: int = RESIDUAL_REFERENCE, stream=None) -> dict:
+    """approximate_two_norm with its internals: lo, up, theta, nb_iter, alpha, beta."""
+    n = _check_mat(A, "A")
+    lo, up, theta = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    nb = ctypes.c_int64()
+    m = max(int(max_iter), 1)
+    alpha = (ctypes.c_double * m)()
+    beta = (ctypes.c_double * m)()
+    st = _capi.lib().psdgb_two_norm_ex(ctypes.c_void_p(A.data_ptr()), n, ctypes.byref(lo), ctypes.byref(up),
+                                       max_iter, tol, seed, residual, None, 0, _stream_ptr(stream), alpha, beta,
+                                       ctypes.byref(nb), ctypes.byref(theta))
+    _capi.check(st, "psdgb_two_norm_ex")
+    k = min(int(max_iter), n)
+    return {"lo": lo.value, "up": up.value, "theta": theta.value, "nb_iter": nb.value,
+            "alpha": list(alpha[:k]), "beta": list(beta[:k])}
+
+
+def approximate_two_norm(A, max_iter: int = 20, tol: float = 1e-10, seed: int = DEFAULT_SEED,
+                         residual: int = RESIDUAL_REFERENCE, stream=None) -> tuple[float, float]:
+    """approximate_two_norm (include/psd_projection/lanczos.h:11-17): returns (lo, up)."""
+    d = lanczos_details(A, max_iter, tol, seed, residual, stream)
+    return d["lo"], d["up"]
+
+
+def _eig(fp64: int, mat, return_eigenvalues: bool, stream=None):
+    torch = _torch()
+    n = _check_mat(mat)
+    eigs = torch.empty(n, dtype=torch.float64, device=mat.device) if return_eigenvalues else None
+    st = _capi.lib().psdgb_eig_psd(fp64, ctypes.c_void_p(mat.data_ptr()), n,
+                                   ctypes.c_void_p(eigs.data_ptr()) if eigs is not None else None,
+                                   _stream_ptr(stream))
+    _capi.check(st, "psdgb_eig_psd")
+    return eigs
+
+
+def eig_FP64_psd(mat, return_eigenvalues: bool = False):
+    """eig_FP64_psd (include/psd_projection/eig_FP64_psd.h:14-20): in place; optional eigenvalues."""
+    return _eig(1, mat, return_eigenvalues)
+
+
+def eig_FP32_psd(mat, return_eigenvalues: bool = False):
+    return _eig(0, mat, return_eigenvalues)
+
+
+def project(method: str, mat, stream=None):
+    """MATLAB psd_projection_MATLAB(A, method) on a device tensor, in place.
+
+    Returns the eigenvalues for eig_* methods, else None."""
+    torch = _torch()
+    n = _check_mat(mat)
+    eigs = None
+    if method in ("eig_FP64", "eig_FP32"):
+        eigs = torch.empty(n, dtype=torch.float64, device=mat.device)
+    st = _capi.lib().psdgb_project(method.encode(), ctypes.c_void_p(mat.data_ptr()), n,
+                                   ctypes.c_void_p(eigs.data_ptr()) if eigs is not None else None,
+                                   _stream_ptr(stream))
+    _capi.check(st, "psdgb_project")
+    return eigs
+
+
+def project_host(method: str, a, out=None, stream=None):
+    """psd_projection_MATLAB(A, method) on host memory: a is an (n, n) float64
+    numpy array (or pinned CPU tensor) read as column-major; the projection is
+    written to out (a new array when None).  Returns (out, eigenvalues|None)."""
+    import numpy as np
+
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        src_ptr, n = a.data_ptr(), a.shape[0]
+        if out is None:
+            out = torch.empty_like(a)
+        dst_ptr = out.data_ptr()
+    else:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        n = a.shape[0]
+        if out is None:
+            out = np.empty_like(a)
+        src_ptr, dst_ptr = a.ctypes.data, out.ctypes.data
+    eigs = np.empty(n, dtype=np.float64) if method in ("eig_FP64", "eig_FP32") else None
+    st = _capi.lib().psdgb_project_host(method.encode(), ctypes.c_void_p(src_ptr), ctypes.c_void_p(dst_ptr), n,
+                                        ctypes.c_void_p(eigs.ctypes.data) if eigs is not None else None,
+                                        _stream_ptr(stream))
+    _capi.check(st, "psdgb_project_host")
+    return out, eigs
+
+
+def kernel_launch_count() -> int:
+    return int(_capi.lib().psdgb_kernel_launch_count())
+
+
+def rel_frobenius(a, b, stream=None) -> float:
+    """||a - b||_F / ||b||_F of two n x n float64 CUDA tensors (FP64 reduction on the device)."""
+    n = _check_mat(a, "a")
+    _check_mat(b, "b")
+    out = ctypes.c_double()
+    st = _capi.lib().psdgb_rel_frobenius(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()), n,
+                                         ctypes.byref(out), _stream_ptr(stream))
+    _capi.check(st, "psdgb_rel_frobenius")
+    return out.value

@@ -1,0 +1,503 @@
+// capi.cu — the extern "C" entry points of libpsdgb.so (declared in include/psdgb.h).
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "internal.h"
+
+namespace psdgb {
+
+size_t composite_ws_bytes(int64_t n, int precision);
+psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                           bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                           void* lz_state, cudaStream_t s, double* up_out);
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+std::mutex g_mu;                         // guards g_states and the cached workspaces
+std::map<int, DeviceState*> g_states;   // one per device, kept until exit
+std::recursive_mutex g_call_mu;          // one library call at a time uses the cached workspaces
+
+constexpr uint64_t kDefaultSeed = 0x5eed5eedull;
+
+// Product timing state (psdgb_product_timing_*).
+struct TimingState {
+    bool on = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending, spare;
+    std::vector<double> pending_flops;
+    double ms = 0.0, flops = 0.0;
+    uint64_t launches = 0;
+    cudaEvent_t cur = nullptr;
+};
+TimingState g_timing;
+std::mutex g_timing_mu;
+
+// Grow-only cached device buffer.
+psdgb_status ensure_buffer(void** ptr, size_t* have, size_t need) {
+    if (*have >= need && *ptr != nullptr) return PSDGB_OK;
+    if (*ptr) {
+        cudaDeviceSynchronize();
+        cudaFree(*ptr);
+        *ptr = nullptr;
+        *have = 0;
+    }
+    if (need == 0) return PSDGB_OK;
+    cudaError_t e = cudaMalloc(ptr, need);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        set_error(std::string("workspace allocation of ") + std::to_string(need) + " bytes failed: " +
+                  cudaGetErrorString(e));
+        return PSDGB_ERR_OUT_OF_MEMORY;
+    }
+    *have = need;
+    return PSDGB_OK;
+}
+
+struct Handles {
+    cublasHandle_t blas = nullptr;
+    cusolverDnHandle_t solver = nullptr;
+};
+Handles& handles_for_device(int dev) {
+    static std::map<int, Handles> hs;
+    std::lock_guard<std::mutex> lk(g_mu);
+    Handles& h = hs[dev];
+    if (!h.blas) cublasCreate(&h.blas);
+    if (!h.solver) cusolverDnCreate(&h.solver);
+    return h;
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+psdgb_status cuda_fail(cudaError_t e, const char* what) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? PSDGB_ERR_OUT_OF_MEMORY : PSDGB_ERR_CUDA;
+}
+
+void count_launch(uint64_t k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
+psdgb_status device_state(DeviceState** out) {
+    int dev = 0;
+    PSDGB_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_states.find(dev);
+    if (it != g_states.end()) {
+        *out = it->second;
+        return PSDGB_OK;
+    }
+    DeviceState* ds = new DeviceState();
+    ds->device = dev;
+    cudaDeviceProp prop;
+    PSDGB_CUDA_TRY(cudaGetDeviceProperties(&prop, dev));
+    ds->sm_count = prop.multiProcessorCount;
+    ds->cc_major = prop.major;
+    ds->cc_minor = prop.minor;
+    PSDGB_CUDA_TRY(cudaMalloc(&ds->d_error, 256));
+    PSDGB_CUDA_TRY(cudaMemset(ds->d_error, 0, 256));
+    g_states[dev] = ds;
+    *out = ds;
+    return PSDGB_OK;
+}
+
+void product_timing_begin(cudaStream_t s) {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    if (!g_timing.on) return;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!g_timing.spare.empty()) {
+        e0 = g_timing.spare.back().first;
+        e1 = g_timing.spare.back().second;
+        g_timing.spare.pop_back();
+    } else {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+    }
+    cudaEventRecord(e0, s);
+    g_timing.pending.push_back({e0, e1});
+    g_timing.pending_flops.push_back(0.0);
+}
+
+void product_timing_end(cudaStream_t s, double mma_flops) {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    if (!g_timing.on || g_timing.pending.empty()) return;
+    cudaEventRecord(g_timing.pending.back().second, s);
+    g_timing.pending_flops.back() = mma_flops;
+}
+
+void product_timing_collect() {
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    for (size_t i = 0; i < g_timing.pending.size(); ++i) {
+        float ms = 0.f;
+        cudaEventSynchronize(g_timing.pending[i].second);
+        if (cudaEventElapsedTime(&ms, g_timing.pending[i].first, g_timing.pending[i].second) == cudaSuccess) {
+            g_timing.ms += ms;
+            g_timing.flops += g_timing.pending_flops[i];
+            g_timing.launches += 1;
+        }
+        g_timing.spare.push_back(g_timing.pending[i]);
+    }
+    g_timing.pending.clear();
+    g_timing.pending_flops.clear();
+}
+
+psdgb_status finish(DeviceState* ds, cudaStream_t stream) {
+    PSDGB_CUDA_TRY(cudaStreamSynchronize(stream));
+    product_timing_collect();
+    int code = 0;
+    PSDGB_CUDA_TRY(cudaMemcpy(&code, ds->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (code != DEVERR_NONE) {
+        PSDGB_CUDA_TRY(cudaMemset(ds->d_error, 0, sizeof(int)));
+        set_error("a bounded device-side wait gave up (device error " + std::to_string(code) + ")");
+        return PSDGB_ERR_DEVICE_TIMEOUT;
+    }
+    return PSDGB_OK;
+}
+
+}  // namespace psdgb
+
+using namespace psdgb;
+
+namespace {
+
+psdgb_status require_sm103(DeviceState* ds) {
+    if (!(ds->cc_major == 10 && ds->cc_minor == 3)) {
+        set_error("psdgb kernels are built for sm_103a; device has compute capability " +
+                  std::to_string(ds->cc_major) + "." + std::to_string(ds->cc_minor));
+        return PSDGB_ERR_UNSUPPORTED;
+    }
+    return PSDGB_OK;
+}
+
+// Resolve the composite workspace: the caller's when large enough, else the cache.
+psdgb_status resolve_ws(DeviceState* ds, int64_t n, int precision, void* d_ws, size_t ws_bytes, void** out) {
+    const size_t need = composite_ws_bytes(n, precision);
+    if (d_ws != nullptr && ws_bytes >= need) {
+        *out = d_ws;
+        return PSDGB_OK;
+    }
+    PSDGB_TRY(ensure_buffer(&ds->ws, &ds->ws_bytes, need));
+    *out = ds->ws;
+    return PSDGB_OK;
+}
+
+psdgb_status resolve_lz(DeviceState* ds, int64_t n, int64_t max_iter, void** out) {
+    PSDGB_TRY(ensure_buffer(&ds->lz, &ds->lz_bytes, lanczos_state_bytes(n, max_iter)));
+    *out = ds->lz;
+    return PSDGB_OK;
+}
+
+psdgb_status do_eig(DeviceState* ds, int fp64, double* d_mat, int64_t n, double* d_eigs_out, cudaStream_t s) {
+    if (n == 0) return PSDGB_OK;
+    Handles& h = handles_for_device(ds->device);
+    if (cusolverDnSetStream(h.solver, s) != CUSOLVER_STATUS_SUCCESS || cublasSetStream(h.blas, s) != CUBLAS_STATUS_SUCCESS) {
+        set_error("cuSOLVER/cuBLAS set stream failed");
+        return PSDGB_ERR_SOLVER;
+    }
+    const int in = static_cast<int>(n);
+    const size_t nn = static_cast<size_t>(n) * n;
+    int* d_info = nullptr;
+    PSDGB_CUDA_TRY(cudaMalloc(&d_info, sizeof(int)));
+    psdgb_status st = PSDGB_OK;
+    if (fp64) {
+        // src/eig_FP64_psd.cu:24-85: syevd (upper) -> clip -> V diag(max(w,0)) V^T.
+        double *V = nullptr, *W = nullptr, *work = nullptr, *VS = nullptr;
+        int lwork = 0;
+        if (cudaMalloc(&V, nn * 8) || cudaMalloc(&VS, nn * 8) || cudaMalloc(&W, n * 8)) {
+            st = PSDGB_ERR_OUT_OF_MEMORY;
+        } else {
+            cudaMemcpyAsync(V, d_mat, nn * 8, cudaMemcpyDeviceToDevice, s);
+            cusolverDnDsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in, W, &lwork);
+            if (cudaMalloc(&work, sizeof(double) * (lwork > 0 ? lwork : 1))) st = PSDGB_ERR_OUT_OF_MEMORY;
+        }
+        if (st == PSDGB_OK &&
+            cusolverDnDsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in, W, work, lwork,
+                             d_info) != CUSOLVER_STATUS_SUCCESS)
+            st = PSDGB_ERR_SOLVER;
+        if (st == PSDGB_OK) {
+            if (d_eigs_out) cudaMemcpyAsync(d_eigs_out, W, n * 8, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(VS, V, nn * 8, cudaMemcpyDeviceToDevice, s);
+            if (launch_scale_columns_relu(VS, W, n, s) != cudaSuccess) st = PSDGB_ERR_CUDA;
+            const double one = 1.0, zero = 0.0;
+            if (st == PSDGB_OK && cublasDgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, V, in, &zero,
+                                              d_mat, in) != CUBLAS_STATUS_SUCCESS)
+                st = PSDGB_ERR_SOLVER;
+        }
+        cudaStreamSynchronize(s);
+        cudaFree(V); cudaFree(VS); cudaFree(W); cudaFree(work);
+    } else {
+        // src/eig_FP32_psd.cu:23-96: FP32 copy -> Ssyevd -> clip -> V diag V^T -> FP64.
+        float *A = nullptr, *VS = nullptr, *W = nullptr, *work = nullptr, *C = nullptr;
+        int lwork = 0;
+        if (cudaMalloc(&A, nn * 4) || cudaMalloc(&VS, nn * 4) || cudaMalloc(&C, nn * 4) || cudaMalloc(&W, n * 4)) {
+            st = PSDGB_ERR_OUT_OF_MEMORY;
+        } else {
+            launch_f64_to_f32(d_mat, A, static_cast<int64_t>(nn), s);
+            cusolverDnSsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in, W, &lwork);
+            if (cudaMalloc(&work, sizeof(float) * (lwork > 0 ? lwork : 1))) st = PSDGB_ERR_OUT_OF_MEMORY;
+        }
+        if (st == PSDGB_OK &&
+            cusolverDnSsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in, W, work, lwork,
+                             d_info) != CUSOLVER_STATUS_SUCCESS)
+            st = PSDGB_ERR_SOLVER;
+        if (st == PSDGB_OK) {
+            if (d_eigs_out) launch_f32_to_f64(W, d_eigs_out, n, s);
+            cudaMemcpyAsync(VS, A, nn * 4, cudaMemcpyDeviceToDevice, s);
+            if (launch_scale_columns_relu_f32(VS, W, n, s) != cudaSuccess) st = PSDGB_ERR_CUDA;
+            const float one = 1.0f, zero = 0.0f;
+            if (st == PSDGB_OK && cublasSgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, A, in, &zero,
+                                              C, in) != CUBLAS_STATUS_SUCCESS)
+                st = PSDGB_ERR_SOLVER;
+            if (st == PSDGB_OK) launch_f32_to_f64(C, d_mat, static_cast<int64_t>(nn), s);
+        }
+        cudaStreamSynchronize(s);
+        cudaFree(A); cudaFree(VS); cudaFree(C); cudaFree(W); cudaFree(work);
+    }
+    if (st == PSDGB_OK) {
+        int info = 0;
+        cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost);
+        if (info != 0) {
+            set_error("syevd reported info = " + std::to_string(info));
+            st = PSDGB_ERR_SOLVER;
+        }
+    } else if (st == PSDGB_ERR_OUT_OF_MEMORY) {
+        set_error("eig: device allocation failed");
+        cudaGetLastError();
+    } else if (st == PSDGB_ERR_SOLVER) {
+        set_error("eig: cuSOLVER/cuBLAS call failed");
+    }
+    cudaFree(d_info);
+    return st;
+}
+
+bool method_precision(const char* method, int* precision, int* schedule, int* eig64) {
+    *eig64 = -1;
+    if (!method) return false;
+    if (!std::strcmp(method, "composite_FP16")) { *precision = PSDGB_PREC_FP16; *schedule = PSDGB_SCHEDULE_FP16; return true; }
+    if (!std::strcmp(method, "composite_FP32")) { *precision = PSDGB_PREC_FP16X3; *schedule = PSDGB_SCHEDULE_FP32; return true; }
+    if (!std::strcmp(method, "composite_FP32_emulated")) { *precision = PSDGB_PREC_BF16X9; *schedule = PSDGB_SCHEDULE_FP32; return true; }
+    if (!std::strcmp(method, "eig_FP64")) { *eig64 = 1; return true; }
+    if (!std::strcmp(method, "eig_FP32")) { *eig64 = 0; return true; }
+    return false;
+}
+
+}  // namespace
+
+extern "C" {
+
+int psdgb_version(void) { return 10000; }
+
+const char* psdgb_last_error(void) { return g_last_error.c_str(); }
+
+const char* psdgb_precision_name(int precision) {
+    switch (precision) {
+        case PSDGB_PREC_FP32_SIMT: return "fp32_simt";
+        case PSDGB_PREC_FP16: return "fp16";
+        case PSDGB_PREC_BF16: return "bf16";
+        case PSDGB_PREC_FP16X3: return "fp16x3";
+        case PSDGB_PREC_BF16X3: return "bf16x3";
+        case PSDGB_PREC_BF16X6: return "bf16x6";
+        case PSDGB_PREC_BF16X9: return "bf16x9";
+        default: return nullptr;
+    }
+}
+
+size_t psdgb_composite_workspace_size(int64_t n, int precision) { return composite_ws_bytes(n, precision); }
+
+psdgb_status psdgb_release_workspace(void) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    std::lock_guard<std::mutex> lk(g_mu);
+    cudaDeviceSynchronize();
+    for (auto& kv : g_states) {
+        DeviceState* ds = kv.second;
+        if (ds->ws) cudaFree(ds->ws);
+        if (ds->lz) cudaFree(ds->lz);
+        ds->ws = ds->lz = nullptr;
+        ds->ws_bytes = ds->lz_bytes = 0;
+    }
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_composite(int precision, int schedule, double* d_mat, int64_t n, void* d_ws, size_t ws_bytes,
+                             void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (n > 0 && d_mat == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void* ws = nullptr;
+    if (n > 0) PSDGB_TRY(resolve_ws(ds, n, precision, d_ws, ws_bytes, &ws));
+    PSDGB_TRY(composite_run(ds, precision, schedule, d_mat, n, ws, false, 0, 0.0, 0, 0, nullptr, s, nullptr));
+    return finish(ds, s);
+}
+
+psdgb_status psdgb_composite_auto_scale(int precision, int schedule, double* d_mat, int64_t n, int64_t max_iter,
+                                        double tol, uint64_t seed, int residual_mode, void* d_ws, size_t ws_bytes,
+                                        void* stream, double* up_out) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (n > 0 && d_mat == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (max_iter < 0) { set_error("max_iter must be >= 0"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void *ws = nullptr, *lz = nullptr;
+    if (n > 0) {
+        PSDGB_TRY(resolve_ws(ds, n, precision, d_ws, ws_bytes, &ws));
+        PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
+    }
+    PSDGB_TRY(composite_run(ds, precision, schedule, d_mat, n, ws, true, max_iter, tol, seed, residual_mode, lz, s,
+                            up_out));
+    return finish(ds, s);
+}
+
+psdgb_status psdgb_two_norm_ex(const double* d_A, int64_t n, double* lo, double* up, int64_t max_iter, double tol,
+                               uint64_t seed, int residual_mode, void* d_ws, size_t ws_bytes, void* stream,
+                               double* h_alpha, double* h_beta, int64_t* nb_iter, double* theta) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (!lo || !up) { set_error("lo/up must not be null"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n < 0 || max_iter < 0) { set_error("n and max_iter must be >= 0"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n > 0 && d_A == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    LanczosResult lr;
+    if (n > 0) {
+        const int64_t ld = (n + 3) / 4 * 4;
+        const size_t a32_bytes = sizeof(float) * static_cast<size_t>(n) * ld;
+        void* a32 = nullptr;
+        if (d_ws != nullptr && ws_bytes >= a32_bytes) {
+            a32 = d_ws;
+        } else {
+            PSDGB_TRY(ensure_buffer(&ds->ws, &ds->ws_bytes, a32_bytes));
+            a32 = ds->ws;
+        }
+        void* lz = nullptr;
+        PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
+        PSDGB_CUDA_TRY(launch_sym_upper_to_f32(d_A, n, static_cast<float*>(a32), ld, s));
+        PSDGB_TRY(lanczos_bound(ds, static_cast<float*>(a32), n, ld, max_iter, tol, seed, residual_mode, lz, s, &lr,
+                                h_alpha, h_beta));
+    }
+    *lo = lr.lo;
+    *up = lr.up;
+    if (nb_iter) *nb_iter = lr.nb_iter;
+    if (theta) *theta = lr.theta;
+    return finish(ds, s);
+}
+
+psdgb_status psdgb_two_norm(const double* d_A, int64_t n, double* lo, double* up, int64_t max_iter, double tol,
+                            uint64_t seed, int residual_mode, void* d_ws, size_t ws_bytes, void* stream) {
+    return psdgb_two_norm_ex(d_A, n, lo, up, max_iter, tol, seed, residual_mode, d_ws, ws_bytes, stream, nullptr,
+                             nullptr, nullptr, nullptr);
+}
+
+psdgb_status psdgb_eig_psd(int fp64, double* d_mat, int64_t n, double* d_eigs_out, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (n < 0 || n > 2147483647LL) { set_error("bad matrix size"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n > 0 && d_mat == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PSDGB_TRY(do_eig(ds, fp64, d_mat, n, d_eigs_out, s));
+    return finish(ds, s);
+}
+
+psdgb_status psdgb_project(const char* method, double* d_mat, int64_t n, double* d_eigs_out, void* stream) {
+    int precision = 0, schedule = 0, eig64 = -1;
+    if (!method_precision(method, &precision, &schedule, &eig64)) {
+        set_error("Unknown method. Supported methods: 'composite_FP16', 'composite_FP32', "
+                  "'composite_FP32_emulated', 'eig_FP64', and 'eig_FP32'.");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (eig64 >= 0) return psdgb_eig_psd(eig64, d_mat, n, d_eigs_out, stream);
+    return psdgb_composite_auto_scale(precision, schedule, d_mat, n, 20, 1e-10, kDefaultSeed, PSDGB_RESIDUAL_REFERENCE,
+                                      nullptr, 0, stream, nullptr);
+}
+
+psdgb_status psdgb_project_host(const char* method, const double* h_in, double* h_out, int64_t n, double* h_eigs_out,
+                                void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    int precision = 0, schedule = 0, eig64 = -1;
+    if (!method_precision(method, &precision, &schedule, &eig64)) {
+        set_error("Unknown method. Supported methods: 'composite_FP16', 'composite_FP32', "
+                  "'composite_FP32_emulated', 'eig_FP64', and 'eig_FP32'.");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n < 0) { set_error("bad matrix size"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n == 0) return PSDGB_OK;
+    if (!h_in || !h_out) { set_error("null host buffer"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n) * n;
+    // The staging matrix (and the eigenvalue vector) live in a cached buffer
+    // after the composite workspace so repeated calls allocate nothing.
+    static void* stage = nullptr;
+    static size_t stage_bytes = 0;
+    const size_t need = bytes + sizeof(double) * static_cast<size_t>(n) + 256;
+    PSDGB_TRY(ensure_buffer(&stage, &stage_bytes, need));
+    double* d_mat = static_cast<double*>(stage);
+    double* d_eigs = reinterpret_cast<double*>(static_cast<char*>(stage) + (bytes + 255) / 256 * 256);
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(d_mat, h_in, bytes, cudaMemcpyHostToDevice, s));
+    psdgb_status st = psdgb_project(method, d_mat, n, h_eigs_out ? d_eigs : nullptr, stream);
+    if (st != PSDGB_OK) return st;
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(h_out, d_mat, bytes, cudaMemcpyDeviceToHost, s));
+    if (h_eigs_out && eig64 >= 0)
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(h_eigs_out, d_eigs, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
+    return PSDGB_OK;
+}
+
+uint64_t psdgb_kernel_launch_count(void) { return g_launches.load(); }
+
+psdgb_status psdgb_product_timing_enable(int on) {
+    product_timing_collect();
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    g_timing.on = on != 0;
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_product_timing_read(double* ms, uint64_t* launches, double* mma_flops, int reset) {
+    product_timing_collect();
+    std::lock_guard<std::mutex> lk(g_timing_mu);
+    if (ms) *ms = g_timing.ms;
+    if (launches) *launches = g_timing.launches;
+    if (mma_flops) *mma_flops = g_timing.flops;
+    if (reset) {
+        g_timing.ms = 0.0;
+        g_timing.flops = 0.0;
+        g_timing.launches = 0;
+    }
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_rel_frobenius(const double* d_a, const double* d_b, int64_t n, double* out, void* stream) {
+    if (!out || n < 0) { set_error("bad arguments"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* d2 = nullptr;
+    PSDGB_CUDA_TRY(cudaMalloc(&d2, 2 * sizeof(double)));
+    cudaError_t e = launch_diff_norms(d_a, d_b, n * n, d2, s);
+    double h2[2] = {0.0, 0.0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h2, d2, sizeof(h2), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d2);
+    if (e != cudaSuccess) return cuda_fail(e, "rel_frobenius");
+    *out = h2[1] > 0.0 ? std::sqrt(h2[0] / h2[1]) : std::sqrt(h2[0]);
+    return PSDGB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,247 @@
+// common.cuh — shared device helpers for the psdgb kernels (sm_103a only).
+//
+// Holds the operand-split arithmetic used by every kernel that writes filter
+// operands, the inline-PTX wrappers for mbarrier / TMA / tcgen05, and the
+// bounded-wait helpers.  Every spin-wait in this library is bounded by a
+// wall-clock limit read from %globaltimer; a wait that gives up records an
+// error code in the library's device error word and the kernel returns.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+namespace psdgb {
+
+// ---------------------------------------------------------------------------
+// Storage formats of a filter operand ("split matrix").
+//   F32  : one FP32 term (plain SIMT mode).
+//   F16  : two FP16 terms, x = hi + lo.
+//   BF16 : three BF16 terms, x = b0 + b1 + b2 (Henry, Tang & Heinecke,
+//          "Leveraging the bfloat16 AI datatype for higher-precision
+//          computations", ARITH 2019).
+// ---------------------------------------------------------------------------
+enum Format : int { FMT_F32 = 0, FMT_F16 = 1, FMT_BF16 = 2 };
+
+struct SplitMat {
+    void* term[3];   // device pointers, each Np x Np row-major (ld = Np), zero padded
+};
+
+__host__ __device__ inline int format_terms(int fmt) { return fmt == FMT_F32 ? 1 : (fmt == FMT_F16 ? 2 : 3); }
+__host__ __device__ inline int format_elem_bytes(int fmt) { return fmt == FMT_F32 ? 4 : 2; }
+
+#if defined(__CUDACC__)
+// Read the value a split matrix stores at linear index idx (FP32 sum of terms).
+__device__ __forceinline__ float split_load(const SplitMat& m, int fmt, size_t idx) {
+    if (fmt == FMT_F32) return static_cast<const float*>(m.term[0])[idx];
+    if (fmt == FMT_F16) {
+        const __half* h = static_cast<const __half*>(m.term[0]);
+        const __half* l = static_cast<const __half*>(m.term[1]);
+        return __half2float(h[idx]) + __half2float(l[idx]);
+    }
+    const __nv_bfloat16* b0 = static_cast<const __nv_bfloat16*>(m.term[0]);
+    const __nv_bfloat16* b1 = static_cast<const __nv_bfloat16*>(m.term[1]);
+    const __nv_bfloat16* b2 = static_cast<const __nv_bfloat16*>(m.term[2]);
+    return __bfloat162float(b0[idx]) + (__bfloat162float(b1[idx]) + __bfloat162float(b2[idx]));
+}
+
+// Split an FP32 value into its terms and store them at linear index idx.
+__device__ __forceinline__ void split_store(const SplitMat& m, int fmt, size_t idx, float v) {
+    if (fmt == FMT_F32) { static_cast<float*>(m.term[0])[idx] = v; return; }
+    if (fmt == FMT_F16) {
+        __half h = __float2half_rn(v);
+        __half l = __float2half_rn(v - __half2float(h));
+        static_cast<__half*>(m.term[0])[idx] = h;
+        static_cast<__half*>(m.term[1])[idx] = l;
+        return;
+    }
+    __nv_bfloat16 b0 = __float2bfloat16_rn(v);
+    float r1 = v - __bfloat162float(b0);
+    __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+    __nv_bfloat16 b2 = __float2bfloat16_rn(r1 - __bfloat162float(b1));
+    static_cast<__nv_bfloat16*>(m.term[0])[idx] = b0;
+    static_cast<__nv_bfloat16*>(m.term[1])[idx] = b1;
+    static_cast<__nv_bfloat16*>(m.term[2])[idx] = b2;
+}
+
+#endif  // __CUDACC__
+
+// ---------------------------------------------------------------------------
+// Epilogue of a symmetric product C = P * Q.  Only the elements (p, q) with
+// p >= q (row-major view; the upper triangle of the column-major matrix) are
+// computed; each is written at (p, q) and mirrored to (q, p).
+// ---------------------------------------------------------------------------
+enum EpiKind : int {
+    EPI_STORE = 0,  // C -> out (split)
+    EPI_STEP = 1,   // a*A + b*A3 + c*acc -> out (split); A, A3 read from split matrices
+    EPI_FINAL = 2   // 0.5*(X + up*acc) -> out64 (FP64, n x n, ld n); X read from x64
+};
+
+struct EpiParams {
+    int kind;
+    int fmt;          // format of the split matrices below
+    int np;           // padded dimension (multiple of 128)
+    int n;            // true dimension
+    float a, b, c;    // EPI_STEP coefficients
+    double up;        // EPI_FINAL scale
+    SplitMat out;     // EPI_STORE / EPI_STEP destination (may alias A for EPI_STEP)
+    SplitMat A;       // EPI_STEP inputs
+    SplitMat A3;
+    const double* x64;  // EPI_FINAL input X (n x n)
+    double* out64;      // EPI_FINAL output (may alias x64)
+    int dual;           // mainloop: accumulate P*Q^T + Q*P^T (K doubled), the symmetric part of the product
+    float acc_scale;    // EPI_FINAL: the accumulator is multiplied by this (0.5 for a dual product)
+};
+
+// ---------------------------------------------------------------------------
+// Error word and bounded waits.
+// ---------------------------------------------------------------------------
+enum DeviceError : int {
+    DEVERR_NONE = 0,
+    DEVERR_TMA_WAIT = 1,     // producer gave up waiting for a free stage
+    DEVERR_MMA_WAIT = 2,     // MMA warp gave up waiting for loaded operands
+    DEVERR_EPI_WAIT = 3,     // epilogue gave up waiting for the accumulator
+    DEVERR_DRAIN_WAIT = 4    // in-flight copies/MMAs did not drain after an abort
+};
+
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wall-clock limit of a single device-side wait.  Every legitimate wait in
+// these kernels lasts microseconds to a few milliseconds.
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// ---- mbarrier -------------------------------------------------------------
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Wait for the phase with the given parity to complete; false after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
+
+// ---- TMA ------------------------------------------------------------------
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, uint64_t* bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+            smem_u32(smem_dst)),
+        "l"(tmap), "r"(smem_u32(bar)), "r"(x), "r"(y)
+        : "memory");
+}
+__device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(tmap) : "memory");
+}
+
+// ---- tcgen05 --------------------------------------------------------------
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Allocate ncols TMEM columns (power of two >= 32); one full warp executes it.
+__device__ __forceinline__ void tmem_alloc(uint32_t* smem_result, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(smem_result)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, both K-major, kind::f16 (FP16 or BF16 in, FP32 out).
+__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Arrive on an mbarrier once every tcgen05 op issued so far by this thread completes.
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Load 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor of a K-major tile written by TMA with
+// 128-byte swizzle: rows of 128 bytes, 8-row swizzle atoms 1024 bytes apart.
+// Fields (tcgen05 shared memory descriptor): start address >> 4 in bits 0-13,
+// leading byte offset >> 4 in bits 16-29 (unused for swizzled K-major),
+// stride byte offset >> 4 in bits 32-45, descriptor version 1 in bits 46-47,
+// base offset 0 (atoms are 1024-byte aligned), swizzle mode 2 (128B) in bits 61-63.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(1u) << 16;
+    d |= static_cast<uint64_t>(1024u >> 4) << 32;
+    d |= static_cast<uint64_t>(1u) << 46;
+    d |= static_cast<uint64_t>(2u) << 61;
+    return d;
+}
+
+#endif  // __CUDACC__
+
+// Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator
+// (bits 4-5 = 1), A/B format in bits 7-9 / 10-12 (0 = FP16, 1 = BF16),
+// both operands K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool bf16) {
+    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) |
+           (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
+}
+
+}  // namespace psdgb

@@ -1,0 +1,253 @@
+// composite.cu — host orchestration of the composite polynomial filter.
+//
+// Restates the control flow of composite_FP32 / composite_FP16 /
+// composite_FP32_emulated (src/composite_FP32.cu:15-164,
+// src/composite_FP16.cu:16-246, src/composite_FP32_emulated.cu:20-235) and
+// their _auto_scale wrappers (src/composite_FP32.cu:166-191 and the FP16 /
+// emulated twins), on the fused kernels of this library:
+//
+//   prologue  FP64 input -> FP32 copy for the Lanczos bound -> scaled operand
+//             terms (padded to a multiple of 128, zero padding);
+//   per step  A2 = A*A; A3 = A2*A; A = a*A + b*A3 + c*A3*A2   (three products,
+//             the coefficient combination fused into the third epilogue);
+//   final     out = (X + up * (Xs*A + A*Xs)/2) / 2 with Xs = X / up, fused into
+//             the last product's epilogue, written in FP64 in place — the same
+//             matrix as the reference's sym(Xs * (I + A) / 2) times up
+//             (:142-156, :190).  The symmetric part is one K-concatenated
+//             product on one triangle: [Xs | A] * [A | Xs]^T.
+//
+// Workspace: three split matrices (A, A2, A3) of Np x Np, Np = n rounded up
+// to 128.  The FP32 copy the Lanczos bound streams lives in A2's storage
+// (A2 is not in use until the first product), and the final product's Xs
+// operand is written into A2's storage as well.
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace psdgb {
+
+namespace {
+
+// Quintic coefficients (a, b, c) of the sign filter, src/composite_FP32.cu:73-84
+// ("polar express refined", 10 steps; also src/composite_FP32_emulated.cu:78-89).
+const double kCoeffFP32[10][3] = {
+    {8.3119043343, -23.0739115930, 16.4664144722}, {4.1439360087, -2.9176674704, 0.5246212487},
+    {4.0257813209, -2.9025002398, 0.5334261214},   {3.5118574347, -2.5740236523, 0.5050097282},
+    {2.4398158400, -1.7586675341, 0.4191290613},   {1.9779835097, -1.3337358510, 0.3772169049},
+    {1.9559726949, -1.3091355170, 0.3746734515},   {1.9282822454, -1.2823649693, 0.3704626545},
+    {1.9220135179, -1.2812524618, 0.3707011753},   {1.8942192942, -1.2613293407, 0.3676616051}};
+// src/composite_FP16.cu:93-101 ("polar express with refinement", 7 steps).
+const double kCoeffFP16[7][3] = {
+    {8.2885332412, -22.5927099246, 15.8201383114}, {4.1666196466, -2.9679004036, 0.5307623217},
+    {4.0611848147, -2.9698947955, 0.5492133813},   {3.6678301399, -2.7561018955, 0.5421513305},
+    {2.7632556383, -2.0607754898, 0.4695405857},   {2.0527445797, -1.4345145882, 0.4070669182},
+    {1.8804816691, -1.2583997294, 0.3779501813}};
+
+}  // namespace
+
+struct Step {
+    float a, b, c;
+};
+
+// The per-step coefficients after the safety scaling p(x / s), computed in
+// FP32 exactly as the reference does (src/composite_FP32.cu:86-99: s = 1.001
+// on steps 0-7; src/composite_FP16.cu:103-113: s = 1.01 on every step).
+std::vector<Step> schedule_steps(int schedule) {
+    std::vector<Step> out;
+    if (schedule == PSDGB_SCHEDULE_FP16) {
+        const float s = 1.01f;
+        for (auto& r : kCoeffFP16) {
+            float a = static_cast<float>(r[0]), b = static_cast<float>(r[1]), c = static_cast<float>(r[2]);
+            a /= s;
+            b /= s * s * s;
+            c /= s * s * s * s * s;
+            out.push_back({a, b, c});
+        }
+    } else {
+        const float s = 1.001f;
+        for (int i = 0; i < 10; ++i) {
+            float a = static_cast<float>(kCoeffFP32[i][0]), b = static_cast<float>(kCoeffFP32[i][1]),
+                  c = static_cast<float>(kCoeffFP32[i][2]);
+            if (i < 8) {
+                a /= s;
+                b /= s * s * s;
+                c /= s * s * s * s * s;
+            }
+            out.push_back({a, b, c});
+        }
+    }
+    return out;
+}
+
+namespace {
+
+struct Layout {
+    int fmt;
+    int64_t np;
+    size_t mat_bytes;
+    SplitMat A, A2, A3;
+    float* a32;   // FP32 copy of the input (n x ld), inside A2's storage
+    int64_t ld;   // = n rounded up to 4
+};
+
+Layout make_layout(void* ws, int fmt, int64_t n) {
+    Layout L{};
+    L.fmt = fmt;
+    L.np = pad128(n);
+    const size_t term = static_cast<size_t>(L.np) * L.np * format_elem_bytes(fmt);
+    const int nt = format_terms(fmt);
+    L.mat_bytes = term * nt;
+    char* base = static_cast<char*>(ws);
+    SplitMat* mats[3] = {&L.A, &L.A2, &L.A3};
+    for (int m = 0; m < 3; ++m) {
+        for (int t = 0; t < 3; ++t) mats[m]->term[t] = (t < nt) ? base + m * L.mat_bytes + t * term : nullptr;
+    }
+    L.a32 = reinterpret_cast<float*>(L.A2.term[0]);
+    L.ld = (n + 3) / 4 * 4;
+    return L;
+}
+
+EpiParams epi_base(const Layout& L, int64_t n) {
+    EpiParams ep{};
+    ep.fmt = L.fmt;
+    ep.np = static_cast<int>(L.np);
+    ep.n = static_cast<int>(n);
+    return ep;
+}
+
+psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layout& L, int64_t n, cudaStream_t s) {
+    for (const Step& st : schedule_steps(schedule)) {
+        EpiParams e1 = epi_base(L, n);
+        e1.kind = EPI_STORE;
+        e1.out = L.A2;
+        PSDGB_TRY(gemm_symmetric(ds, precision, L.A, L.A, L.np, e1, s));  // A2 = A * A
+        EpiParams e2 = epi_base(L, n);
+        e2.kind = EPI_STORE;
+        e2.out = L.A3;
+        PSDGB_TRY(gemm_symmetric(ds, precision, L.A2, L.A, L.np, e2, s));  // A3 = A2 * A
+        EpiParams e3 = epi_base(L, n);
+        e3.kind = EPI_STEP;
+        e3.a = st.a;
+        e3.b = st.b;
+        e3.c = st.c;
+        e3.A = L.A;
+        e3.A3 = L.A3;
+        e3.out = L.A;
+        PSDGB_TRY(gemm_symmetric(ds, precision, L.A3, L.A2, L.np, e3, s));  // A = aA + bA3 + cA3*A2
+    }
+    return PSDGB_OK;
+}
+
+// mat (in place) = (X + up * Xs * A) / 2, Xs = X / up, X read from mat.
+psdgb_status run_final(DeviceState* ds, int precision, const Layout& L, double* mat, int64_t n, double up,
+                       cudaStream_t s) {
+    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0 / up, L.A2, L.fmt, L.np, s));
+    EpiParams ef = epi_base(L, n);
+    ef.kind = EPI_FINAL;
+    ef.up = up;
+    // (Xs*A + A*Xs)/2: the symmetric part of the product, as the reference's
+    // symmetrisation of W does (src/composite_FP32.cu:153).
+    ef.dual = 1;
+    ef.acc_scale = 0.5f;
+    ef.x64 = mat;
+    ef.out64 = mat;
+    return gemm_symmetric(ds, precision, L.A2, L.A, L.np, ef, s);
+}
+
+psdgb_status check_n(int64_t n) {
+    if (n < 0) {
+        set_error("matrix size must be >= 0");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n > 46340 * 2) {  // Np^2 indices and tile counts stay in range
+        set_error("matrix size too large (n <= 92680)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    return PSDGB_OK;
+}
+
+}  // namespace
+
+bool precision_info(int precision, PrecisionInfo* out) {
+    switch (precision) {
+        case PSDGB_PREC_FP32_SIMT: *out = {FMT_F32, 0, 1}; return true;
+        case PSDGB_PREC_FP16: *out = {FMT_F16, 1, 1}; return true;
+        case PSDGB_PREC_BF16: *out = {FMT_BF16, 1, 1}; return true;
+        case PSDGB_PREC_FP16X3: *out = {FMT_F16, 3, 2}; return true;
+        case PSDGB_PREC_BF16X3: *out = {FMT_BF16, 3, 2}; return true;
+        case PSDGB_PREC_BF16X6: *out = {FMT_BF16, 6, 3}; return true;
+        case PSDGB_PREC_BF16X9: *out = {FMT_BF16, 9, 3}; return true;
+        default: return false;
+    }
+}
+
+size_t split_matrix_bytes(int fmt, int64_t np) {
+    return static_cast<size_t>(np) * np * format_elem_bytes(fmt) * format_terms(fmt);
+}
+
+psdgb_status gemm_symmetric(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                            const EpiParams& ep, cudaStream_t s) {
+    PrecisionInfo pi{};
+    precision_info(precision, &pi);
+    const double nt = static_cast<double>(np / 128);
+    const double flops = nt * (nt + 1) / 2 * 2.0 * 128 * 128 * static_cast<double>(np) * (ep.dual ? 2 : 1) *
+                         (pi.nprod > 0 ? pi.nprod : 1);
+    product_timing_begin(s);
+    psdgb_status st = (precision == PSDGB_PREC_FP32_SIMT) ? gemm_simt(ds, P, Q, np, ep, s)
+                                                           : gemm_tc(ds, precision, P, Q, np, ep, s);
+    product_timing_end(s, flops);
+    return st;
+}
+
+size_t composite_ws_bytes(int64_t n, int precision) {
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi) || n <= 0) return 0;
+    return 3 * split_matrix_bytes(pi.fmt, pad128(n));
+}
+
+psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                           bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                           void* lz_state, cudaStream_t s, double* up_out) {
+    PSDGB_TRY(check_n(n));
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi)) {
+        set_error("unknown precision");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) {
+        set_error("unknown schedule");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (up_out) *up_out = 1.0;
+    if (n == 0) return PSDGB_OK;
+    const Layout L = make_layout(ws, pi.fmt, n);
+    double up = 1.0;
+    if (auto_scale) {
+        PSDGB_CUDA_TRY(launch_sym_upper_to_f32(mat, n, L.a32, L.ld, s));
+        LanczosResult lr;
+        PSDGB_TRY(lanczos_bound(ds, L.a32, n, L.ld, max_iter, tol, seed, residual_mode, lz_state, s, &lr, nullptr,
+                                nullptr));
+        up = lr.up > 0.0 ? lr.up : 1.0;  // src/composite_FP32.cu:182
+        PSDGB_CUDA_TRY(launch_split_from_f32(L.a32, n, L.ld, 1.0 / up, L.A, L.fmt, L.np, s));
+    } else {
+        PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, L.A, L.fmt, L.np, s));
+    }
+    PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s));
+    PSDGB_TRY(run_final(ds, precision, L, mat, n, up, s));
+    if (up_out) *up_out = up;
+    return PSDGB_OK;
+}
+
+}  // namespace psdgb
+
+extern "C" int psdgb_filter_coefficients(int schedule, float* out, int cap) {
+    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) return -1;
+    const std::vector<psdgb::Step> steps = psdgb::schedule_steps(schedule);
+    for (int i = 0; i < cap && i < static_cast<int>(steps.size()); ++i) {
+        out[3 * i] = steps[i].a;
+        out[3 * i + 1] = steps[i].b;
+        out[3 * i + 2] = steps[i].c;
+    }
+    return static_cast<int>(steps.size());
+}

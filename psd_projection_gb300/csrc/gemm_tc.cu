@@ -1,0 +1,428 @@
+// gemm_tc.cu — symmetric filter products on the sm_103a tensor cores.
+//
+// Replaces the reference's cublasSgemm / cublasGemmEx chain
+// (src/composite_FP32.cu:103-115,150; src/composite_FP16.cu:118-163,218-227;
+// src/composite_FP32_emulated.cu:108-153,210-221).  Each product C = P * Q of
+// two symmetric, commuting matrices is computed on the 128x128 tiles (bi, bj)
+// with bi >= bj only, so half the MMA work of a full GEMM.
+//
+// Kernel structure (one output tile per CTA, 192 threads):
+//   warp 0 lane 0  TMA producer: per 64-wide K block, loads the operand term
+//                  tiles of P (rows of tile bi) and Q (rows of tile bj) into a
+//                  STAGES-deep shared-memory ring (128-byte swizzle, K-major);
+//   warp 1 lane 0  MMA issuer: tcgen05.mma kind::f16 (FP16 or BF16 in, FP32
+//                  accumulate in TMEM), one MMA per term product per 16-wide
+//                  K slice; tcgen05.commit frees ring stages and signals the
+//                  accumulator;
+//   warps 2-5      epilogue: tcgen05.ld of the 128x128 FP32 accumulator (one
+//                  TMEM lane per tile row), the polynomial step / ReLU
+//                  reconstruction, operand splitting, and the stores at (p, q)
+//                  and at the mirror (q, p).
+// Because P and Q are symmetric, the B operand "Q^T" is Q itself, so both
+// operands are K-major row blocks of row-major matrices.
+//
+// Split precision: an operand x is stored as terms (FP16 hi + lo, or BF16
+// b0 + b1 + b2); the product is the sum of the term products selected by
+// the precision (1, 3, 6 or 9), all accumulated in the same FP32 TMEM tile.
+//
+// Every mbarrier wait is bounded (common.cuh); a wait that gives up records a
+// DeviceError, drains the copies and MMAs it issued, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "epilogue.cuh"
+#include "internal.h"
+
+namespace psdgb {
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int TILE_BYTES = BM * BK * 2;  // one operand term tile: 128 rows x 128 bytes
+constexpr int THREADS = 192;
+constexpr uint32_t TMEM_COLS = 128;
+
+template <int TERMS>
+struct TcCfg {
+    static constexpr int STAGES = TERMS == 1 ? 6 : (TERMS == 2 ? 3 : 2);
+    static constexpr int STAGE_BYTES = 2 * TERMS * TILE_BYTES;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+};
+
+struct alignas(64) TmapSet {
+    CUtensorMap P[3];
+    CUtensorMap Q[3];
+};
+
+// Term product list: product i multiplies term prod_a(i) of P by term
+// prod_b(i) of Q.  The first 1 / 3 / 6 / 9 products are the x1 / x3 / x6 / x9
+// schemes: (0,0); (0,1), (1,0); (0,2), (2,0), (1,1); (1,2), (2,1), (2,2).
+__host__ __device__ constexpr int prod_a(int i) {
+    return i == 2 ? 1 : i == 4 ? 2 : i == 5 ? 1 : i == 6 ? 1 : i == 7 ? 2 : i == 8 ? 2 : 0;
+}
+__host__ __device__ constexpr int prod_b(int i) {
+    return i == 1 ? 1 : i == 3 ? 2 : i == 5 ? 1 : i == 6 ? 2 : i == 7 ? 1 : i == 8 ? 2 : 0;
+}
+
+__device__ __forceinline__ void tri_decode(int64_t t, int64_t& bi, int64_t& bj) {
+    int64_t i = static_cast<int64_t>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    bi = i;
+    bj = t - i * (i + 1) / 2;
+}
+
+__device__ __forceinline__ void record_error(int* err, volatile int* abort_flag, int code) {
+    *abort_flag = 1;
+    atomicCAS(err, 0, code);
+}
+
+// ---- epilogue helpers ------------------------------------------------------
+
+// Store 32 consecutive values of row p (columns q0..q0+31) and their mirrors.
+// full: every element of the run satisfies p > q (no diagonal masking).
+template <int FMT>
+__device__ __forceinline__ void store_run(const SplitMat& m, int64_t np, int64_t p, int64_t q0, const float (&v)[32],
+                                          bool full) {
+    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+    const size_t row_idx = static_cast<size_t>(p) * np + q0;
+    if (full) {
+        // Direct row store: 32 elements x 2 bytes per term = four 16-byte vectors.
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            uint32_t packed[16];
+            // Recompute the term t of each element (cheap; keeps registers low).
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                float x0 = v[j], x1 = v[j + 1];
+                uint16_t h0 = 0, h1 = 0;
+#pragma unroll
+                for (int u = 0; u <= t; ++u) {
+                    if (FMT == FMT_F16) {
+                        __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
+                        h0 = __half_as_ushort(a0);
+                        h1 = __half_as_ushort(a1);
+                        x0 -= __half2float(a0);
+                        x1 -= __half2float(a1);
+                    } else {
+                        __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
+                        h0 = __bfloat16_as_ushort(a0);
+                        h1 = __bfloat16_as_ushort(a1);
+                        x0 -= __bfloat162float(a0);
+                        x1 -= __bfloat162float(a1);
+                    }
+                }
+                packed[j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
+            }
+            uint4* dst = reinterpret_cast<uint4*>(static_cast<uint16_t*>(m.term[t]) + row_idx);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+        }
+#pragma unroll
+        for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(q0 + j) * np + p, v[j]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int64_t q = q0 + j;
+            if (p >= q) {
+                split_store(m, FMT, row_idx + j, v[j]);
+                if (p != q) split_store(m, FMT, static_cast<size_t>(q) * np + p, v[j]);
+            }
+        }
+    }
+}
+
+template <int FMT>
+__device__ __forceinline__ void load_run(const SplitMat& m, size_t idx, float (&out)[32]) {
+    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) out[j] = 0.f;
+    // Sum the terms from the smallest to the largest.
+#pragma unroll
+    for (int t = NT - 1; t >= 0; --t) {
+        const uint4* src = reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(m.term[t]) + idx);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint4 w = src[u];
+            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int h = 0; h < 4; ++h) {
+                const uint16_t lo = static_cast<uint16_t>(ws[h] & 0xFFFFu), hi = static_cast<uint16_t>(ws[h] >> 16);
+                float f0, f1;
+                if (FMT == FMT_F16) {
+                    f0 = __half2float(__ushort_as_half(lo));
+                    f1 = __half2float(__ushort_as_half(hi));
+                } else {
+                    f0 = __bfloat162float(__ushort_as_bfloat16(lo));
+                    f1 = __bfloat162float(__ushort_as_bfloat16(hi));
+                }
+                out[8 * u + 2 * h] += f0;
+                out[8 * u + 2 * h + 1] += f1;
+            }
+        }
+    }
+}
+
+template <int FMT>
+__device__ void epilogue_tile(const EpiParams& ep, uint32_t tmem_row, int64_t p, int64_t bj) {
+    const int64_t np = ep.np;
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
+        const int64_t q0 = bj * BN + c0;
+        if (q0 > p) continue;  // whole run above the diagonal: owned by the mirror tile
+        if (ep.kind == EPI_FINAL) {
+            if (p >= ep.n) continue;
+            const int64_t n = ep.n;
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+                const int64_t q = q0 + j;
+                if (q <= p && q < n) {
+                    const double x = ep.x64[p * n + q];
+                    const double o = 0.5 * (x + ep.up * static_cast<double>(ep.acc_scale * v[j]));
+                    ep.out64[p * n + q] = o;
+                    if (q != p) ep.out64[q * n + p] = o;
+                }
+            }
+            continue;
+        }
+        const size_t idx = static_cast<size_t>(p) * np + q0;
+        if (ep.kind == EPI_STEP) {
+            float a[32], a3[32];
+            load_run<FMT>(ep.A, idx, a);
+            load_run<FMT>(ep.A3, idx, a3);
+#pragma unroll
+            for (int j = 0; j < 32; ++j) v[j] = fmaf(ep.c, v[j], fmaf(ep.b, a3[j], ep.a * a[j]));
+        }
+        store_run<FMT>(ep.out, np, p, q0, v, p > q0 + 31);
+    }
+}
+
+// ---- the kernel --------------------------------------------------------------
+
+template <int TERMS, int NPROD, bool BF16>
+__global__ void __launch_bounds__(THREADS, 1)
+    tc_sym_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, int num_kb, int* err) {
+    using Cfg = TcCfg<TERMS>;
+    constexpr int STAGES = Cfg::STAGES;
+    constexpr int STAGE_BYTES = Cfg::STAGE_BYTES;
+    constexpr uint32_t IDESC = idesc_f16(BM, BN, BF16);
+
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw_addr = smem_u32(smem_raw);
+    uint8_t* smem = smem_raw + ((1024u - (raw_addr & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+    uint64_t* empty = full + STAGES;
+    uint64_t* accf = empty + STAGES;
+    uint64_t* drain = accf + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* issued_slot = abort_flag + 1;
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    int64_t bi, bj;
+    tri_decode(blockIdx.x, bi, bj);
+    const int num_kb_half = num_kb;          // K blocks of one product
+    if (ep.dual) num_kb = 2 * num_kb;        // K blocks of the whole mainloop
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accf, 1);
+        mbar_init(drain, 1);
+        *abort_flag = 0;
+        *issued_slot = 0;
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, TMEM_COLS);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        // ---- TMA producer ----
+        for (int t = 0; t < TERMS; ++t) {
+            tma_prefetch_desc(&tm.P[t]);
+            tma_prefetch_desc(&tm.Q[t]);
+        }
+        int issued = 0;
+        for (int kb = 0; kb < num_kb; ++kb) {
+            const int s = kb % STAGES;
+            const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
+            if (!mbar_wait_bounded(&empty[s], ph ^ 1u)) {
+                record_error(err, abort_flag, DEVERR_TMA_WAIT);
+                break;
+            }
+            if (*abort_flag) break;
+            uint8_t* st = smem + s * STAGE_BYTES;
+            // In a dual product the second half of the K loop multiplies Q's
+            // rows bi by P's rows bj (the transpose-side term Q * P^T).
+            const bool second = kb >= num_kb_half;
+            const CUtensorMap* mp = second ? tm.Q : tm.P;
+            const CUtensorMap* mq = second ? tm.P : tm.Q;
+            const int kx = (second ? kb - num_kb_half : kb) * BK;
+            mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+#pragma unroll
+            for (int t = 0; t < TERMS; ++t)
+                tma_load_2d(st + t * TILE_BYTES, &mp[t], &full[s], kx, static_cast<int>(bi * BM));
+#pragma unroll
+            for (int t = 0; t < TERMS; ++t)
+                tma_load_2d(st + (TERMS + t) * TILE_BYTES, &mq[t], &full[s], kx, static_cast<int>(bj * BN));
+            issued = kb + 1;
+        }
+        *issued_slot = issued;
+    } else if (warp == 1 && lane == 0) {
+        // ---- MMA issuer ----
+        bool ok = true;
+        for (int kb = 0; kb < num_kb; ++kb) {
+            const int s = kb % STAGES;
+            const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
+            if (!mbar_wait_bounded(&full[s], ph)) {
+                record_error(err, abort_flag, DEVERR_MMA_WAIT);
+                ok = false;
+                break;
+            }
+            if (*abort_flag) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+#pragma unroll
+            for (int k = 0; k < BK / 16; ++k) {
+#pragma unroll
+                for (int pi = 0; pi < NPROD; ++pi) {
+                    const uint64_t ad = sdesc_kmajor_sw128(base + prod_a(pi) * TILE_BYTES + k * 32);
+                    const uint64_t bd = sdesc_kmajor_sw128(base + (TERMS + prod_b(pi)) * TILE_BYTES + k * 32);
+                    umma_f16(tmem, ad, bd, IDESC, (kb | k | pi) != 0 ? 1u : 0u);
+                }
+            }
+            umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(accf);
+    } else if (warp >= 2) {
+        // ---- epilogue ----
+        const int q4 = warp & 3;  // TMEM lane quarter this warp may access
+        const int64_t p = bi * BM + q4 * 32 + lane;
+        if (!mbar_wait_bounded(accf, 0)) {
+            record_error(err, abort_flag, DEVERR_EPI_WAIT);
+        } else if (!*abort_flag) {
+            tc_fence_after();
+            const uint32_t tmem_row = tmem + (static_cast<uint32_t>(q4 * 32) << 16);
+            if (ep.fmt == FMT_F16)
+                epilogue_tile<FMT_F16>(ep, tmem_row, p, bj);
+            else
+                epilogue_tile<FMT_BF16>(ep, tmem_row, p, bj);
+        }
+    }
+
+    // ---- teardown ----
+    tc_fence_before();
+    __syncthreads();
+    if (*abort_flag) {
+        if (warp == 1 && lane == 0) {
+            // Wait until every MMA issued so far has completed.
+            umma_commit(drain);
+            if (!mbar_wait_bounded(drain, 0)) atomicCAS(err, 0, DEVERR_DRAIN_WAIT);
+        }
+        if (warp == 0 && lane == 0) {
+            // Wait for the loads of the last STAGES issued K blocks to land.
+            const int issued = *issued_slot;
+            for (int kb = issued - STAGES; kb < issued; ++kb) {
+                if (kb < 0) continue;
+                const int s = kb % STAGES;
+                const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
+                if (!mbar_wait_bounded(&full[s], ph)) atomicCAS(err, 0, DEVERR_DRAIN_WAIT);
+            }
+        }
+        __syncthreads();
+    }
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// ---- host side -------------------------------------------------------------
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+bool make_tmap(CUtensorMap* tm, void* base, int64_t np, bool bf16) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(np), static_cast<cuuint64_t>(np)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(np) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BM)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r =
+        fn(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box,
+           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+template <int TERMS, int NPROD, bool BF16>
+psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t np, const EpiParams& ep,
+                       cudaStream_t s) {
+    using Cfg = TcCfg<TERMS>;
+    static bool configured = false;  // attribute set once per process (per instantiation)
+    if (!configured) {
+        PSDGB_CUDA_TRY(cudaFuncSetAttribute(tc_sym_kernel<TERMS, NPROD, BF16>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
+        configured = true;
+    }
+    TmapSet tm;
+    for (int t = 0; t < 3; ++t) {
+        void* pb = (t < TERMS) ? P.term[t] : P.term[0];
+        void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
+        if (!make_tmap(&tm.P[t], pb, np, BF16) || !make_tmap(&tm.Q[t], qb, np, BF16)) {
+            set_error("cuTensorMapEncodeTiled failed");
+            return PSDGB_ERR_CUDA;
+        }
+    }
+    const int64_t nt = np / BM;
+    const int64_t tiles = nt * (nt + 1) / 2;
+    const int num_kb = static_cast<int>(np / BK);
+    tc_sym_kernel<TERMS, NPROD, BF16>
+        <<<static_cast<unsigned>(tiles), THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, num_kb, ds->d_error);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    return PSDGB_OK;
+}
+
+}  // namespace
+
+psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                     const EpiParams& ep, cudaStream_t s) {
+    switch (precision) {
+        case PSDGB_PREC_FP16: return launch_tc<1, 1, false>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16: return launch_tc<1, 1, true>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_FP16X3: return launch_tc<2, 3, false>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16X3: return launch_tc<2, 3, true>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16X6: return launch_tc<3, 6, true>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16X9: return launch_tc<3, 9, true>(ds, P, Q, np, ep, s);
+        default: break;
+    }
+    set_error("gemm_tc: unknown precision");
+    return PSDGB_ERR_INVALID_ARGUMENT;
+}
+
+}  // namespace psdgb

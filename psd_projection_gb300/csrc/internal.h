@@ -1,0 +1,108 @@
+// internal.h — host-side declarations shared by the psdgb translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "psdgb.h"
+
+namespace psdgb {
+
+// ---- error reporting (capi.cu) ----------------------------------------------
+void set_error(const std::string& msg);
+psdgb_status cuda_fail(cudaError_t e, const char* what);
+void count_launch(uint64_t k = 1);
+
+#define PSDGB_CUDA_TRY(expr)                                      \
+    do {                                                          \
+        cudaError_t _e = (expr);                                  \
+        if (_e != cudaSuccess) return ::psdgb::cuda_fail(_e, #expr); \
+    } while (0)
+
+#define PSDGB_TRY(expr)                           \
+    do {                                          \
+        psdgb_status _s = (expr);                 \
+        if (_s != PSDGB_OK) return _s;            \
+    } while (0)
+
+// Per-device state: a small device buffer holding the error word of the
+// bounded waits, plus cached workspaces.
+struct DeviceState {
+    int device = -1;
+    int* d_error = nullptr;  // device error word (DeviceError)
+    void* ws = nullptr;      // cached composite workspace
+    size_t ws_bytes = 0;
+    void* lz = nullptr;      // cached Lanczos state
+    size_t lz_bytes = 0;
+    int sm_count = 0;
+    int cc_major = 0, cc_minor = 0;
+};
+psdgb_status device_state(DeviceState** out);
+// Synchronise the stream and turn a device error word into a status.
+psdgb_status finish(DeviceState* ds, cudaStream_t stream);
+
+// ---- product timing (capi.cu) --------------------------------------------------
+// Record an event before / after a product launch when timing is enabled.
+void product_timing_begin(cudaStream_t s);
+void product_timing_end(cudaStream_t s, double mma_flops);
+// Fold the finished event pairs into the totals (after a stream sync).
+void product_timing_collect();
+
+// ---- precision helpers (composite.cu) -------------------------------------------
+struct PrecisionInfo {
+    int fmt;        // storage Format of the operands
+    int nprod;      // products per term pair list (1, 3, 6, 9); 0 for SIMT
+    int terms;      // operand terms read by the products
+};
+bool precision_info(int precision, PrecisionInfo* out);
+inline int64_t pad128(int64_t n) { return (n + 127) / 128 * 128; }
+size_t split_matrix_bytes(int fmt, int64_t np);
+
+// ---- elementwise kernels (elem.cu) --------------------------------------------
+// a32 (n x ld, ld = pad4(n), zero padded) = FP32 of the symmetric matrix
+// defined by the upper triangle of the column-major FP64 matrix x.
+cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s);
+// out (Np x Np split matrix) = split(scale * a32), zero padding.
+cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const SplitMat& out,
+                                  int fmt, int64_t np, cudaStream_t s);
+// out (Np x Np split matrix) = split(scale * sym_upper(x)), zero padding.
+cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const SplitMat& out, int fmt,
+                                        int64_t np, cudaStream_t s);
+// FP64 reductions: out[0] = sum (a-b)^2, out[1] = sum b^2 over n*n elements.
+cudaError_t launch_diff_norms(const double* a, const double* b, int64_t count, double* d_out2, cudaStream_t s);
+// Scale column j of v (n x n col-major FP64) by max(w[j], 0).
+cudaError_t launch_scale_columns_relu(double* v, const double* w, int64_t n, cudaStream_t s);
+cudaError_t launch_scale_columns_relu_f32(float* v, const float* w, int64_t n, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const double* in, float* out, int64_t count, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const float* in, double* out, int64_t count, cudaStream_t s);
+
+// ---- symmetric products (gemm_simt.cu, gemm_tc.cu) -----------------------------
+// C = P * Q for symmetric P, Q (Np x Np split matrices); the epilogue ep
+// consumes C.  precision selects the kernel and the term products.
+psdgb_status gemm_symmetric(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                            const EpiParams& ep, cudaStream_t s);
+psdgb_status gemm_simt(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t np, const EpiParams& ep,
+                       cudaStream_t s);
+psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                     const EpiParams& ep, cudaStream_t s);
+
+// ---- Lanczos (lanczos.cu) ---------------------------------------------------------
+struct LanczosResult {
+    double lo = 0.0, up = 1.0, theta = 0.0;
+    int64_t nb_iter = 0;
+};
+size_t lanczos_state_bytes(int64_t n, int64_t max_iter);
+// Runs the bound on a32 (n x ld FP32, symmetric).  h_alpha / h_beta may be null.
+psdgb_status lanczos_bound(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter, double tol,
+                           uint64_t seed, int residual_mode, void* d_state, cudaStream_t s, LanczosResult* res,
+                           double* h_alpha, double* h_beta);
+
+// ---- host tridiagonal solver (tridiag.cpp) ------------------------------------------
+// Largest eigenvalue of the symmetric tridiagonal matrix (diag d[0..m),
+// off-diagonal e[0..m-1)) and a unit eigenvector for it.
+void tridiag_largest_eigenpair(const double* d, const double* e, int64_t m, double* theta, double* vec);
+
+}  // namespace psdgb

@@ -1,0 +1,341 @@
+// lanczos.cu — spectral-norm bound by Lanczos on A^T A (approximate_two_norm).
+//
+// Follows src/lanczos.cu:41-293 of the reference step for step:
+//   * start vector uniform in (0, 1], normalised (:69,:101-107);
+//   * three-term recurrence without reorthogonalisation (:116-169):
+//       w = A^T A q; alpha_k = q.w; w -= alpha_k q + beta_{k-1} q_old;
+//       beta_k = ||w||; stop if beta_k <= tol*alpha_k and k > 1, or beta_k == 0;
+//   * theta = largest eigenvalue of the tridiagonal T (:186-231), Ritz vector
+//     y = V u (:236-242), residual r, lo = sqrt(theta), up = sqrt(theta + ||r||)
+//     (:244-270).  The reference's residual is r = A y - theta y (its copy at
+//     :255 runs ry -> w1, leaving ry = A y); PSDGB_RESIDUAL_EXACT uses
+//     r = A^T A y - theta y instead.
+//
+// GB300 design: the matrix is streamed as FP32 (4 n^2 bytes per matvec
+// instead of the reference's 8 n^2 per Dgemv, two per step), one warp per
+// column with 128-bit loads and warp-shuffle reductions, FP64 for every
+// reduction and every vector; the recurrence runs on the device (no host
+// round trip per step) and the host reads alpha/beta once at the end.  The
+// start vector comes from a counter-based hash (SplitMix64) of a caller seed
+// instead of the reference's nondeterministic curand seed (src/utils.cu:188-214).
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace psdgb {
+
+namespace {
+
+struct LzState {
+    int nb_iter;
+    int stopped;
+    double beta_old;
+    double resid_norm2;   // sum of squares of the Ritz residual
+};
+
+// Layout of the Lanczos state inside its buffer.
+struct LzLayout {
+    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk;
+    size_t total;
+};
+
+inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+LzLayout lz_layout(int64_t n, int64_t m) {
+    LzLayout L{};
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = align256(off + bytes); return o; };
+    const size_t n4 = static_cast<size_t>((n + 3) / 4 * 4);
+    L.state = take(sizeof(LzState));
+    L.alpha = take(sizeof(double) * (m + 1));
+    L.beta = take(sizeof(double) * (m + 1));
+    L.q = take(sizeof(double) * n);
+    L.w = take(sizeof(double) * n);
+    L.vold = take(sizeof(double) * n);
+    L.V = take(sizeof(double) * n * (m > 0 ? m : 1));
+    L.y = take(sizeof(double) * n);
+    L.ry = take(sizeof(double) * n);
+    L.q32 = take(sizeof(float) * n4);
+    L.u32 = take(sizeof(float) * n4);
+    L.uk = take(sizeof(double) * (m + 1));
+    L.total = off;
+    return L;
+}
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Block-wide FP64 sum (blockDim.x a multiple of 32, <= 1024).  All threads
+// get the result.
+__device__ double block_sum(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x / 32, l = threadIdx.x % 32, nw = blockDim.x / 32;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = (l < nw) ? red[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+// q = uniform(0,1] from the seed, normalised; V[:,0] = q; q_old = 0.
+__global__ void lz_init_kernel(int64_t n, uint64_t seed, LzState* st, double* q, double* vold, double* V,
+                               float* q32) {
+    __shared__ double red[32];
+    double ss = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t h = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
+        const double u = static_cast<double>((h >> 11) + 1) * 0x1.0p-53;  // (0, 1]
+        q[i] = u;
+        ss += u * u;
+    }
+    const double nrm = sqrt(block_sum(ss, red));
+    const double inv = nrm != 0.0 ? 1.0 / nrm : 1.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = q[i] * inv;
+        q[i] = v;
+        V[i] = v;
+        vold[i] = 0.0;
+        q32[i] = static_cast<float>(v);
+    }
+    if (threadIdx.x == 0) {
+        st->nb_iter = 0;
+        st->stopped = 0;
+        st->beta_old = 0.0;
+        st->resid_norm2 = 0.0;
+    }
+}
+
+// y[c] = sum_r A[c*ld + r] * x[r] for every column c of the symmetric FP32
+// matrix A (so y = A x = A^T x).  One warp per column, float4 loads, FP32
+// partial sums per lane, FP64 across lanes.  x is staged in shared memory.
+// Writes y as FP64 (y64) and/or FP32 (y32).
+__global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict__ A, int64_t n, int64_t ld,
+                                                        const float* __restrict__ x, double* __restrict__ y64,
+                                                        float* __restrict__ y32, const LzState* st) {
+    if (st != nullptr && st->stopped) return;
+    extern __shared__ float4 xs4[];
+    float* xs = reinterpret_cast<float*>(xs4);
+    const int64_t ld4 = ld / 4;
+    for (int64_t i = threadIdx.x; i < ld; i += blockDim.x) xs[i] = (i < n) ? x[i] : 0.0f;
+    __syncthreads();
+    const int lane = threadIdx.x % 32;
+    const int64_t warps_total = static_cast<int64_t>(gridDim.x) * (blockDim.x / 32);
+    for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + threadIdx.x / 32; c < n;
+         c += warps_total) {
+        const float4* col = reinterpret_cast<const float4*>(A + c * ld);
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        double acc = 0.0;
+        int64_t k = lane;
+        // Flush the FP32 partials into FP64 every 64 float4 per lane.
+        while (k < ld4) {
+            const int64_t kend = (k + 32 * 64 < ld4) ? k + 32 * 64 : ld4;
+            for (; k < kend; k += 32) {
+                const float4 a = __ldg(col + k);
+                const float4 b = xs4[k];
+                s0 = fmaf(a.x, b.x, s0);
+                s1 = fmaf(a.y, b.y, s1);
+                s2 = fmaf(a.z, b.z, s2);
+                s3 = fmaf(a.w, b.w, s3);
+            }
+            acc += static_cast<double>(s0) + static_cast<double>(s1) + static_cast<double>(s2) +
+                   static_cast<double>(s3);
+            s0 = s1 = s2 = s3 = 0.f;
+        }
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            if (y64) y64[c] = acc;
+            if (y32) y32[c] = static_cast<float>(acc);
+        }
+    }
+}
+
+// One Lanczos update (single block):
+//   alpha_k = q.w; w -= alpha_k q + beta_old q_old; beta_k = ||w||;
+//   stop tests of src/lanczos.cu:145-159; q_old = q; q = w / beta_k;
+//   V[:, k+1] = q when k < m-1; nb_iter++.
+__global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzState* st, double* alpha, double* beta,
+                                 double* q, double* w, double* vold, double* V, float* q32) {
+    if (st->stopped) return;
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += q[i] * w[i];
+    const double a = block_sum(s, red);
+    const double b_old = st->beta_old;
+    s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = w[i] - a * q[i] - b_old * vold[i];
+        w[i] = v;
+        s += v * v;
+    }
+    const double b = sqrt(block_sum(s, red));
+    if (threadIdx.x == 0) {
+        alpha[k] = a;
+        beta[k] = b;
+    }
+    if ((b <= tol * a && k > 1) || b == 0.0) {
+        __syncthreads();
+        if (threadIdx.x == 0) st->stopped = 1;
+        return;
+    }
+    const double inv = 1.0 / b;
+    const bool store_v = (k < m - 1);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double qn = w[i] * inv;
+        vold[i] = q[i];
+        q[i] = qn;
+        q32[i] = static_cast<float>(qn);
+        if (store_v) V[static_cast<int64_t>(k + 1) * n + i] = qn;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        st->beta_old = b;
+        st->nb_iter = k + 1;
+    }
+}
+
+// y = V[:, 0:m] u; y32 = FP32(y).
+__global__ void lz_ritz_kernel(int64_t n, int64_t m, const double* __restrict__ V, const double* __restrict__ u,
+                               double* y, float* y32) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (int64_t j = 0; j < m; ++j) s += V[j * n + i] * u[j];
+        y[i] = s;
+        y32[i] = static_cast<float>(s);
+    }
+}
+
+// resid_norm2 = ||ry - theta y||^2 (single block).
+__global__ void lz_resid_kernel(int64_t n, double theta, const double* ry, const double* y, LzState* st) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double r = ry[i] - theta * y[i];
+        s += r * r;
+    }
+    const double t = block_sum(s, red);
+    if (threadIdx.x == 0) st->resid_norm2 = t;
+}
+
+cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double* y64, float* y32, const LzState* st,
+                   int sm_count, cudaStream_t s) {
+    const size_t smem = sizeof(float) * static_cast<size_t>(ld);
+    const int threads = 256;
+    int64_t blocks = (n + 7) / 8;  // one column per warp
+    const int64_t cap = static_cast<int64_t>(sm_count) * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    lz_matvec_kernel<<<static_cast<unsigned>(blocks), threads, smem, s>>>(A, n, ld, x, y64, y32, st);
+    count_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t lanczos_state_bytes(int64_t n, int64_t max_iter) {
+    const int64_t m = max_iter < n ? max_iter : n;
+    return lz_layout(n, m).total;
+}
+
+psdgb_status lanczos_bound(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter, double tol,
+                           uint64_t seed, int residual_mode, void* d_state, cudaStream_t s, LanczosResult* res,
+                           double* h_alpha, double* h_beta) {
+    const int64_t m = max_iter < n ? max_iter : n;  // src/lanczos.cu:55
+    *res = LanczosResult{};
+    if (h_alpha) for (int64_t i = 0; i < max_iter; ++i) h_alpha[i] = 0.0;
+    if (h_beta) for (int64_t i = 0; i < max_iter; ++i) h_beta[i] = 0.0;
+    if (m <= 0) {  // no iteration: the all-zero branch of src/lanczos.cu:171-184
+        res->lo = 0.0;
+        res->up = 1.0;
+        return PSDGB_OK;
+    }
+    const size_t xs_bytes = sizeof(float) * static_cast<size_t>(ld);
+    if (xs_bytes > 48 * 1024) {
+        if (xs_bytes > 200 * 1024) {
+            set_error("Lanczos bound: n too large for the shared-memory vector stage (n <= 51200)");
+            return PSDGB_ERR_INVALID_ARGUMENT;
+        }
+        PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            static_cast<int>(xs_bytes)));
+    }
+    const LzLayout L = lz_layout(n, m);
+    char* base = static_cast<char*>(d_state);
+    LzState* st = reinterpret_cast<LzState*>(base + L.state);
+    double* alpha = reinterpret_cast<double*>(base + L.alpha);
+    double* beta = reinterpret_cast<double*>(base + L.beta);
+    double* q = reinterpret_cast<double*>(base + L.q);
+    double* w = reinterpret_cast<double*>(base + L.w);
+    double* vold = reinterpret_cast<double*>(base + L.vold);
+    double* V = reinterpret_cast<double*>(base + L.V);
+    double* y = reinterpret_cast<double*>(base + L.y);
+    double* ry = reinterpret_cast<double*>(base + L.ry);
+    float* q32 = reinterpret_cast<float*>(base + L.q32);
+    float* u32 = reinterpret_cast<float*>(base + L.u32);
+    double* uk = reinterpret_cast<double*>(base + L.uk);
+
+    PSDGB_CUDA_TRY(cudaMemsetAsync(alpha, 0, sizeof(double) * (m + 1), s));
+    PSDGB_CUDA_TRY(cudaMemsetAsync(beta, 0, sizeof(double) * (m + 1), s));
+    lz_init_kernel<<<1, 1024, 0, s>>>(n, seed, st, q, vold, V, q32);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+
+    for (int64_t k = 0; k < m; ++k) {
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, nullptr, u32, st, ds->sm_count, s));  // u = A q
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, u32, w, nullptr, st, ds->sm_count, s));    // w = A^T u
+        lz_update_kernel<<<1, 1024, 0, s>>>(n, m, static_cast<int>(k), tol, st, alpha, beta, q, w, vold, V, q32);
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
+    }
+
+    LzState hst{};
+    std::vector<double> ha(m + 1), hb(m + 1);
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(ha.data(), alpha, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(hb.data(), beta, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+    PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h_alpha) for (int64_t i = 0; i < m; ++i) h_alpha[i] = ha[i];
+    if (h_beta) for (int64_t i = 0; i < m; ++i) h_beta[i] = hb[i];
+
+    const int64_t nb = hst.nb_iter;
+    res->nb_iter = nb;
+    if (nb == 0) {
+        res->lo = 0.0;
+        res->up = 1.0;
+        return PSDGB_OK;
+    }
+    double theta = 0.0;
+    std::vector<double> u(nb);
+    tridiag_largest_eigenpair(ha.data(), hb.data(), nb, &theta, u.data());
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(uk, u.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+    {
+        int64_t blocks = (n + 255) / 256;
+        if (blocks > 4096) blocks = 4096;
+        lz_ritz_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(n, nb, V, uk, y, q32);
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
+    }
+    if (residual_mode == PSDGB_RESIDUAL_EXACT) {
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, nullptr, u32, nullptr, ds->sm_count, s));  // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, u32, ry, nullptr, nullptr, ds->sm_count, s));   // A^T A y
+    } else {
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, ry, nullptr, nullptr, ds->sm_count, s));   // A y
+    }
+    lz_resid_kernel<<<1, 1024, 0, s>>>(n, theta, ry, y, st);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+    PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
+    const double rnorm = std::sqrt(hst.resid_norm2);
+    res->theta = theta;
+    res->lo = std::sqrt(theta);
+    res->up = std::sqrt(theta + rnorm);
+    return PSDGB_OK;
+}
+
+}  // namespace psdgb

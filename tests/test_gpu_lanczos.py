@@ -1,0 +1,81 @@
+"""Lanczos bound on the GPU against the oracle and the reference's KAT."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import reference_port as rp
+from tests.gpu_util import gaussian_sym, to_dev, uniform_spectrum
+
+pytestmark = pytest.mark.gpu
+KAT = json.loads((Path(__file__).resolve().parent / "golden" / "kat.json").read_text())
+
+
+@pytest.fixture(scope="module")
+def psd():
+    import psd_projection_gb300 as psd
+
+    return psd
+
+
+@pytest.mark.parametrize("residual", [0, 1])
+def test_kat_two_norm(psd, residual):
+    k = KAT["lanczos_two_norm"]
+    a = np.array(k["matrix"])
+    lo, up = psd.approximate_two_norm(to_dev(a), k["max_iter"], k["tol"], residual=residual)
+    assert lo <= k["two_norm"] + k["two_norm_rounding"]
+    assert k["two_norm"] <= up
+    assert lo <= np.linalg.norm(a, 2) <= up
+
+
+@pytest.mark.parametrize("n,residual", [(257, 0), (257, 1), (1000, 0), (64, 1)])
+def test_parity_with_oracle(psd, n, residual):
+    """Same seed, same recurrence: alpha/beta, nb_iter and the bounds agree with
+    the FP64 oracle run on the FP32-rounded matrix (the GPU streams FP32)."""
+    x = gaussian_sym(n, seed=n)
+    x32 = x.astype(np.float32).astype(np.float64)
+    want = rp.approximate_two_norm(x32, 20, 1e-10, residual=("reference", "exact")[residual])
+    got = psd.lanczos_details(to_dev(x), 20, 1e-10, residual=residual)
+    assert got["nb_iter"] == want["nb_iter"]
+    nb = want["nb_iter"]
+    np.testing.assert_allclose(got["alpha"][:nb], want["alpha"][:nb], rtol=2e-5)
+    np.testing.assert_allclose(got["beta"][:nb], want["beta"][:nb], rtol=2e-4)
+    assert got["lo"] == pytest.approx(want["lo"], rel=1e-6)
+    assert got["up"] == pytest.approx(want["up"], rel=1e-4)
+    sigma = np.linalg.norm(x, 2)
+    assert got["lo"] <= sigma * (1 + 1e-6) and got["up"] >= sigma * (1 - 1e-6)
+
+
+def test_zero_matrix_and_tiny_sizes(psd):
+    lo, up = psd.approximate_two_norm(to_dev(np.zeros((7, 7))))
+    assert (lo, up) == (0.0, 1.0)
+    lo, up = psd.approximate_two_norm(to_dev(np.array([[-3.0]])))
+    want = rp.approximate_two_norm(np.array([[-3.0]]))
+    assert lo == pytest.approx(3.0, rel=1e-12) and up == pytest.approx(want["up"], rel=1e-12)
+    lo, up = psd.approximate_two_norm(to_dev(np.array([[1.0, 2.0], [2.0, -1.0]])), 5)
+    assert lo <= np.sqrt(5.0) * (1 + 1e-7) <= up * (1 + 1e-7)
+
+
+def test_early_stop_rank_one(psd):
+    v = np.random.default_rng(3).standard_normal(50)
+    a = np.outer(v, v)
+    got = psd.lanczos_details(to_dev(a), 20, 1e-10)
+    want = rp.approximate_two_norm(a.astype(np.float32).astype(np.float64), 20, 1e-10)
+    assert got["nb_iter"] == want["nb_iter"] < 20
+    assert got["lo"] == pytest.approx(np.linalg.norm(a, 2), rel=1e-5)
+
+
+def test_nonsymmetric_input_uses_upper_triangle(psd):
+    x = np.random.default_rng(4).standard_normal((90, 90))
+    got = psd.lanczos_details(to_dev(x), 20, 1e-10)
+    ref = psd.lanczos_details(to_dev(rp.sym_upper(x)), 20, 1e-10)
+    assert got == ref
+
+
+def test_seed_changes_start_but_not_the_bound(psd):
+    x = uniform_spectrum(300, 4.0, seed=9)
+    a = psd.lanczos_details(to_dev(x), 20, 1e-10, seed=1, residual=1)
+    b = psd.lanczos_details(to_dev(x), 20, 1e-10, seed=2, residual=1)
+    assert a["alpha"] != b["alpha"]
+    assert a["lo"] == pytest.approx(4.0, rel=1e-3) and b["lo"] == pytest.approx(4.0, rel=1e-3)
