@@ -312,30 +312,38 @@ def _stored(terms: list[np.ndarray]) -> np.ndarray:
     return s
 
 
-def _product(P: list[np.ndarray], Q: list[np.ndarray], prods) -> np.ndarray:
+def _product(P: list[np.ndarray], Q: list[np.ndarray], prods, dual: bool = False) -> np.ndarray:
+    """Symmetric product as the kernels form it: the lower triangle of
+    sum_ab P_a Q_b mirrored (one triangle computed, stored twice), or for a
+    dual product the symmetric part (PQ + QP)/2."""
     acc = np.zeros(P[0].shape, dtype=np.float64)
     for a, b in prods:
         acc += P[a].astype(np.float64) @ Q[b].astype(np.float64)
-    return acc.astype(np.float32)
+    acc = acc.astype(np.float32)
+    if dual:
+        return ((acc.astype(np.float64) + acc.T) * 0.5).astype(np.float32)
+    return np.tril(acc) + np.tril(acc, -1).T
 
 
 def composite_split_model(X: np.ndarray, precision: str = "fp16x3", schedule: str = "fp32",
                           up: float = 1.0) -> np.ndarray:
     """What this library's kernels compute for composite on X with scale up:
     operands split into terms, products summed over the precision's term
-    pairs (accumulated here in FP64, on the GPU in FP32), the step combination
+    pairs (accumulated here in FP64, on the GPU in FP32; one-term modes take
+    the symmetric part of the third product of each step), the step combination
     a*A + b*A3 + c*A3*A2 in FP32 on the stored values, and the final
     0.5 * (X + up * (Xs*A + A*Xs)/2) in FP64."""
     fmt, _, prods = PRECISION_MODEL[precision]
+    one_term = len(prods) == 1 and fmt != "f32"
     X = sym_upper(np.asarray(X, dtype=np.float64))
     Xs32 = (X * (1.0 / up)).astype(np.float32)
     A_t = split_terms(Xs32, fmt)
     for a, b, c in schedule_coefficients(schedule):
         A2_t = split_terms(_product(A_t, A_t, prods), fmt)
         A3_t = split_terms(_product(A2_t, A_t, prods), fmt)
-        acc = _product(A3_t, A2_t, prods)
+        acc = _product(A3_t, A2_t, prods, dual=one_term)  # one-term modes: symmetric part of A3*A2
         A_new = np.float32(c) * acc + (np.float32(b) * _stored(A3_t) + np.float32(a) * _stored(A_t))
         A_t = split_terms(A_new.astype(np.float32), fmt)
-    PA = _product(split_terms(Xs32, fmt), A_t, prods).astype(np.float64)
-    out = 0.5 * (X + up * 0.5 * (PA + PA.T))   # symmetric part, one dual product on the GPU
+    PA = _product(split_terms(Xs32, fmt), A_t, prods, dual=True).astype(np.float64)
+    out = 0.5 * (X + up * PA)   # symmetric part of Xs*A, one dual product on the GPU
     return sym_upper(out)

@@ -91,7 +91,7 @@ struct EpiParams {
     const double* x64;  // EPI_FINAL input X (n x n)
     double* out64;      // EPI_FINAL output (may alias x64)
     int dual;           // mainloop: accumulate P*Q^T + Q*P^T (K doubled), the symmetric part of the product
-    float acc_scale;    // EPI_FINAL: the accumulator is multiplied by this (0.5 for a dual product)
+    float acc_scale;    // the accumulator is multiplied by this first (0.5 for a dual product)
 };
 
 // ---------------------------------------------------------------------------

@@ -113,10 +113,18 @@ EpiParams epi_base(const Layout& L, int64_t n) {
     ep.fmt = L.fmt;
     ep.np = static_cast<int>(L.np);
     ep.n = static_cast<int>(n);
+    ep.acc_scale = 1.0f;
     return ep;
 }
 
 psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layout& L, int64_t n, cudaStream_t s) {
+    PrecisionInfo pi{};
+    precision_info(precision, &pi);
+    // One-term operands round to 11 (FP16) or 8 (BF16) bits; the antisymmetric
+    // part of that rounding error in A3*A2 is pure error, so those modes take
+    // the symmetric part (A3*A2 + A2*A3)/2 as one dual product, as the
+    // reference symmetrises A after every step (src/composite_FP16.cu:166).
+    const bool dual_step = pi.nprod == 1;
     for (const Step& st : schedule_steps(schedule)) {
         EpiParams e1 = epi_base(L, n);
         e1.kind = EPI_STORE;
@@ -134,6 +142,10 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
         e3.A = L.A;
         e3.A3 = L.A3;
         e3.out = L.A;
+        if (dual_step) {
+            e3.dual = 1;
+            e3.acc_scale = 0.5f;
+        }
         PSDGB_TRY(gemm_symmetric(ds, precision, L.A3, L.A2, L.np, e3, s));  // A = aA + bA3 + cA3*A2
     }
     return PSDGB_OK;
@@ -217,6 +229,12 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
     }
     if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) {
         set_error("unknown schedule");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
+        // The FP32 table applies no safety factor on its last two steps; BF16
+        // operand rounding then pushes eigenvalues past 1 and the quintic diverges.
+        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     if (up_out) *up_out = 1.0;

@@ -17,6 +17,7 @@ namespace psdgb {
 // Value the epilogue produces for product element (p, q) with accumulator acc
 // (EPI_STORE / EPI_STEP).
 __device__ __forceinline__ float epi_value(const EpiParams& ep, size_t idx, float acc) {
+    acc *= ep.acc_scale;
     if (ep.kind == EPI_STEP) {
         const float a = split_load(ep.A, ep.fmt, idx);
         const float a3 = split_load(ep.A3, ep.fmt, idx);

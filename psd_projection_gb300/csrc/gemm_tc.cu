@@ -190,6 +190,8 @@ __device__ void epilogue_tile(const EpiParams& ep, uint32_t tmem_row, int64_t p,
             continue;
         }
         const size_t idx = static_cast<size_t>(p) * np + q0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
         if (ep.kind == EPI_STEP) {
             float a[32], a3[32];
             load_run<FMT>(ep.A, idx, a);

@@ -3,15 +3,18 @@ oracle restatement and with the model of the kernels' arithmetic, edge cases.
 
 Tolerances (relative Frobenius unless stated):
   * against FP64 EVD: 1e-4 for the FP32-class precisions (fp32_simt, fp16x3,
-    bf16x6, bf16x9, bf16x3) — the spec bar; 2e-3 for fp16; 3e-2 for bf16
-    (one-term modes, reported not targeted);
+    bf16x6, bf16x9, bf16x3) — the spec bar; 1e-3 for fp16 (the
+    reference's FP16 bar, test/composite_FP16_test.hpp:129); 1e-2 for bf16
+    (a one-term mode the reference does not have, reported not targeted);
   * GPU against the split-arithmetic model on the same input: 3e-5 for
-    FP32-class precisions, 3e-3 for fp16 and 2e-2 for bf16 — the model
-    accumulates in FP64 where the tensor cores accumulate in FP32, and the
-    one-term modes round operands to 11 / 8 bits, so a last-bit difference
-    in an accumulator can flip an operand rounding;
+    fp32_simt / fp16x3 / bf16x6 / bf16x9 and 1e-4 for bf16x3 — the model
+    accumulates in FP64 where the tensor cores accumulate in FP32; 1e-2 (fp16)
+    and 5e-2 (bf16) for the one-term modes, whose 11 / 8-bit operand rounding
+    turns a last-bit accumulator difference into an operand-rounding flip;
   * the reference's own bars: rel <= 1e-3 (test/composite_FP32_test.hpp:121),
-    abs <= 0.1 at lambda in [-10, 10] (:191, :239), KAT elementwise 1e-3 (:76).
+    abs <= 0.1 at lambda in [-10, 10] (:191, :239), KAT elementwise 1e-3 (:76);
+    the reference asserts its KATs on the FP32 path only, so the one-term
+    modes are held to 1e-2 there.
 """
 import json
 from pathlib import Path
@@ -27,12 +30,13 @@ KAT = json.loads((Path(__file__).resolve().parent / "golden" / "kat.json").read_
 
 FP32_CLASS = ["fp32_simt", "fp16x3", "bf16x3", "bf16x6", "bf16x9"]
 ALL = FP32_CLASS + ["fp16", "bf16"]
-EVD_TOL = {"fp16": 2e-3, "bf16": 3e-2}
-MODEL_TOL = {"fp16": 3e-3, "bf16": 2e-2}
+EVD_TOL = {"fp16": 1e-3, "bf16": 1e-2}
+MODEL_TOL = {"fp16": 1e-2, "bf16": 5e-2, "bf16x3": 1e-4}
+KAT_TOL = {"fp16": 1e-2, "bf16": 1e-2}
 
 
 def sched(p):
-    return "fp16" if p == "fp16" else "fp32"
+    return "fp16" if p in ("fp16", "bf16") else "fp32"
 
 
 @pytest.fixture(scope="module")
@@ -55,14 +59,14 @@ def test_kat_deterministic(psd, precision):
     k = KAT["composite_fp32_deterministic"]
     x = np.array(k["input_over_15"]) / 15.0
     out, _ = run(psd, x, precision, auto_scale=False)
-    assert np.abs(out - np.array(k["expected"])).max() <= k["tolerance"]
+    assert np.abs(out - np.array(k["expected"])).max() <= KAT_TOL.get(precision, k["tolerance"])
 
 
 @pytest.mark.parametrize("precision", ALL)
 def test_kat_simple5(psd, precision):
     k = KAT["composite_simple5"]
     out, _ = run(psd, np.diag(k["diagonal"]), precision, auto_scale=True)
-    assert np.abs(out - np.diag(k["expected_diagonal"])).max() <= k["tolerance"]
+    assert np.abs(out - np.diag(k["expected_diagonal"])).max() <= KAT_TOL.get(precision, k["tolerance"])
 
 
 @pytest.mark.parametrize("precision", ALL)
@@ -82,7 +86,7 @@ def test_bar_autoscaled_abs(psd, precision):
     x = uniform_spectrum(1024, 10.0, seed=2)
     proj, _ = rp.eig_psd(x)
     out, up = run(psd, x, precision, auto_scale=True)
-    assert np.linalg.norm(out - proj) <= (0.1 if precision != "fp16" else 1.0)
+    assert np.linalg.norm(out - proj) <= (0.1 if precision != "fp16" else 0.5)
     assert up >= np.linalg.norm(x, 2)
 
 
@@ -116,6 +120,12 @@ def test_autoscale_parity_with_oracle(psd, precision):
     assert rp.rel_frobenius(out, want) <= 3e-5
     proj, _ = rp.eig_psd(x)
     assert rp.rel_frobenius(out, proj) <= 1e-4
+
+
+def test_bf16_one_term_requires_fp16_schedule(psd):
+    t = to_dev(np.eye(8) * 0.5)
+    with pytest.raises(psd.PsdgbError, match="FP16 schedule"):
+        psd.composite(t, psd.PRECISIONS["bf16"], psd.SCHEDULE_FP32, auto_scale=False)
 
 
 def test_empty_and_tiny(psd):
@@ -156,12 +166,12 @@ def test_reference_method_mapping(psd):
     """composite_FP32 / _FP16 / _emulated entry points use fp16x3 / fp16 / bf16x9."""
     x = uniform_spectrum(150, 1.0, seed=12)
     proj, _ = rp.eig_psd(x)
-    for fn, tol in ((psd.composite_FP32, 1e-4), (psd.composite_FP32_emulated, 1e-4), (psd.composite_FP16, 2e-3)):
+    for fn, tol in ((psd.composite_FP32, 1e-4), (psd.composite_FP32_emulated, 1e-4), (psd.composite_FP16, 1.5e-3)):
         t = to_dev(x)
         fn(t)
         assert rp.rel_frobenius(from_dev(t), proj) <= tol
     for fn, tol in ((psd.composite_FP32_auto_scale, 1e-4), (psd.composite_FP32_emulated_auto_scale, 1e-4),
-                    (psd.composite_FP16_auto_scale, 3e-3)):
+                    (psd.composite_FP16_auto_scale, 2e-3)):
         t = to_dev(x * 7.0)
         fn(t)
         assert rp.rel_frobenius(from_dev(t), proj * 7.0) <= tol
