@@ -14,7 +14,7 @@ Tolerances (relative Frobenius unless stated):
   * the reference's own bars: rel <= 1e-3 (test/composite_FP32_test.hpp:121),
     abs <= 0.1 at lambda in [-10, 10] (:191, :239), KAT elementwise 1e-3 (:76);
     the reference asserts its KATs on the FP32 path only, so the one-term
-    modes are held to 1e-2 there.
+    modes are held to 1e-2 (fp16) and 3e-2 (bf16) there.
 """
 import json
 from pathlib import Path
@@ -32,7 +32,7 @@ FP32_CLASS = ["fp32_simt", "fp16x3", "bf16x3", "bf16x6", "bf16x9"]
 ALL = FP32_CLASS + ["fp16", "bf16"]
 EVD_TOL = {"fp16": 1e-3, "bf16": 1e-2}
 MODEL_TOL = {"fp16": 1e-2, "bf16": 5e-2, "bf16x3": 1e-4}
-KAT_TOL = {"fp16": 1e-2, "bf16": 1e-2}
+KAT_TOL = {"fp16": 1e-2, "bf16": 3e-2}
 
 
 def sched(p):
