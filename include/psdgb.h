@@ -106,6 +106,19 @@ psdgb_status psdgb_release_workspace(void);
 psdgb_status psdgb_composite(int precision, int schedule, double* d_mat, int64_t n,
                              void* d_ws, size_t ws_bytes, void* stream);
 
+/* psdgb_composite for callers that cannot allocate device memory (a solver
+ * that reserves the GPU's memory up front, a real-time loop that may not wait
+ * on or fail in the allocator, code running under stream capture): the
+ * operand scratch is a file-scope device array the library reserves at load
+ * time, so this call allocates nothing.  No counterpart in the reference.
+ * Limits: precision PSDGB_PREC_FP16 or PSDGB_PREC_FP16X3 and n <= 512 (the
+ * array is 3 MiB, held on every GPU that loads the library until exit);
+ * larger n returns PSDGB_ERR_INVALID_ARGUMENT.  The first call on a device
+ * looks up the array's address; make it before any stream capture.  All calls
+ * share the array: overlapping calls on the GPU would race (this library
+ * serialises its own calls, each returning after its stream finishes). */
+psdgb_status psdgb_composite_static(int precision, int schedule, double* d_mat, int64_t n, void* stream);
+
 /* Lanczos bound, scale by 1/up, filter, and rescale by up
  * (composite_*_auto_scale).  max_iter = 20 and tol = 1e-10 are the
  * reference's defaults (src/composite_FP32.cu:177-179 uses the defaults of

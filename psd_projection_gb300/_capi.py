@@ -77,6 +77,7 @@ SIGNATURES = {
     "psdgb_composite_workspace_size": (c_size, [c_i64, c_int]),
     "psdgb_release_workspace": (c_int, []),
     "psdgb_composite": (c_int, [c_int, c_int, c_vp, c_i64, c_vp, c_size, c_vp]),
+    "psdgb_composite_static": (c_int, [c_int, c_int, c_vp, c_i64, c_vp]),
     "psdgb_composite_auto_scale": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_u64, c_int, c_vp, c_size,
                                            c_vp, P_dbl]),
     "psdgb_two_norm": (c_int, [c_vp, c_i64, P_dbl, P_dbl, c_i64, c_dbl, c_u64, c_int, c_vp, c_size, c_vp]),

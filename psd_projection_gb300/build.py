@@ -27,7 +27,7 @@ CFLAGS = [
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
 ]
 SOURCES = ["capi.cu", "composite.cu", "elem.cu", "lanczos.cu", "gemm_simt.cu", "gemm_tc.cu", "refapi.cu",
-           "tridiag.cpp"]
+           "static_scratch.cu", "tridiag.cpp"]
 
 
 def nvcc() -> str:
