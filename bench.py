@@ -54,6 +54,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side-by-side", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving session")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--workload", choices=["spectrum", "gaussian"], default="spectrum",
                     help="spectrum: Q diag(lambda) Q^T (the n=8192 configuration); gaussian: (G+G^T)/2 scaled to "
                          "norm ~1, no QR (used for profiling runs, where ncu cannot load torch's linalg library)")
@@ -209,6 +211,92 @@ def dense_equiv_flops(n: int, steps: int) -> float:
 
 
 # ---------------------------------------------------------------------------
+# serving: 64 ADMM-like streams through the library's request loop
+# ---------------------------------------------------------------------------
+
+def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 4096), n_streams: int = 64,
+                  seed: int = 0, max_slots: int = 16, check_error: bool = False) -> dict:
+    """Closed-loop ADMM streams: stream k (n = sizes[k % 4]) waits an
+    exponential think time (mean n_streams / offered_rate), perturbs its
+    matrix by 1e-2 (E + E^T)/2, submits it, and waits for the projection
+    before its next think time.  Returns throughput and latency percentiles."""
+    import heapq
+
+    import numpy as np
+    import torch
+
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.serve import Server
+
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    mats, outs, ns = [], [], []
+    for k in range(n_streams):
+        n = sizes[k % len(sizes)]
+        G = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+        mats.append((0.5 / n ** 0.5) * (G + G.T))
+        outs.append(torch.empty((n, n), dtype=torch.float64, device="cuda"))
+        ns.append(n)
+    torch.cuda.synchronize()
+    mean_think = n_streams / offered_rate
+    lat, lat_by_n, gpu_ms = [], {n: [] for n in sizes}, []
+    with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10) as srv:
+        # warm the per-(slot, n) graphs outside the measured window
+        for k in range(min(n_streams, 2 * len(sizes))):
+            srv.submit(k, mats[k], outs[k])
+        srv.drain()
+        t0 = psd.serve.clock()
+        t_end = t0 + seconds
+        ready = [(t0 + rng.exponential(mean_think), k) for k in range(n_streams)]
+        heapq.heapify(ready)
+        outstanding = 0
+        submitted = completed = 0
+        while True:
+            now = psd.serve.clock()
+            while ready and ready[0][0] <= now and ready[0][0] < t_end:
+                _, k = heapq.heappop(ready)
+                n = ns[k]
+                E = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+                mats[k].add_(E + E.T, alpha=0.5e-2)
+                torch.cuda.current_stream().synchronize()
+                srv.submit(k, mats[k], outs[k])
+                outstanding += 1
+                submitted += 1
+            if not ready and outstanding == 0:
+                break
+            if ready and ready[0][0] >= t_end and outstanding == 0:
+                break
+            for c in srv.poll(wait=False):
+                outstanding -= 1
+                completed += 1
+                dt = c.end_s - c.submit_s
+                lat.append(dt)
+                lat_by_n[c.n].append(dt)
+                gpu_ms.append(c.gpu_ms)
+                if c.end_s < t_end:
+                    heapq.heappush(ready, (c.end_s + rng.exponential(mean_think), c.key))
+            if outstanding and (not ready or ready[0][0] > psd.serve.clock()):
+                time.sleep(0.0001)
+        wall = psd.serve.clock() - t0
+        err = None
+        if check_error:
+            errs = {}
+            for k in range(len(sizes)):  # one stream per size: its last projection against FP64 EVD
+                ref = mats[k].clone()
+                psd.eig_FP64_psd(ref)
+                errs[ns[k]] = psd.rel_frobenius(outs[k], ref)
+            err = errs
+    a = np.array(lat) * 1e3
+    return {"offered_req_s": offered_rate, "throughput_req_s": completed / wall, "completed": completed,
+            "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
+            "p99_ms": float(np.percentile(a, 99)) if len(a) else None,
+            "p50_ms_by_n": {str(n): float(np.percentile(np.array(v) * 1e3, 50)) for n, v in lat_by_n.items() if v},
+            "p99_ms_by_n": {str(n): float(np.percentile(np.array(v) * 1e3, 99)) for n, v in lat_by_n.items() if v},
+            "rel_frobenius_err_by_n": err, "wall_s": wall}
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline: FP64 LAPACK dsyevd projection (eig_FP64_psd's math)
 # ---------------------------------------------------------------------------
 
@@ -354,6 +442,14 @@ def run_ours(args, rank, world):
                           "method": {"fp16": "composite_FP16", "bf16x9": "composite_FP32_emulated",
                                      "fp32_simt": "plain FP32 (CUDA cores)"}.get(name, name)}
         out["side_by_side"] = side
+
+    if not args.no_serve:
+        sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
+        out["serving"] = {
+            "workload": "64 closed-loop ADMM-like streams, n uniform over {64,256,1024,4096} (16 streams each), "
+                        "next matrix = previous + 1e-2 (E+E^T)/2, exponential think time for the offered rate; "
+                        "fp16x3, warm-started Lanczos (10 steps), 16 slots, CUDA-graph replay",
+            "sessions": sessions}
 
     if world == 1 and not args.no_cpu_baseline:
         rate, t, scale = cpu_evd_projection_rate(X, n, args.cpu_sample_n)

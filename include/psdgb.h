@@ -129,6 +129,29 @@ psdgb_status psdgb_composite_auto_scale(int precision, int schedule, double* d_m
                                         void* d_ws, size_t ws_bytes, void* stream,
                                         double* up_out);
 
+/* Bytes of the Lanczos state (a few n-vectors and the n x max_iter basis). */
+size_t psdgb_lanczos_state_size(int64_t n, int64_t max_iter);
+
+/* psdgb_composite_auto_scale without any host synchronisation: the Lanczos
+ * bound, the scale 1/up and the filter are enqueued on `stream` and the call
+ * returns.  Nothing is allocated: the caller provides the filter workspace
+ * (>= psdgb_composite_workspace_size) and the Lanczos state
+ * (>= psdgb_lanczos_state_size) and must not reuse either, or read d_mat,
+ * before the stream has passed this work.  d_warm_start (n doubles, device,
+ * may be NULL) replaces the seeded start vector — e.g. the previous Ritz
+ * vector of a slowly changing matrix; d_ritz_out (n doubles, may be NULL)
+ * receives this call's Ritz vector.  A bounded device wait that gives up is
+ * reported by the next psdgb_check_device_error() (or synchronous call).
+ * The enqueued work can be captured in a CUDA graph. */
+psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, double* d_mat, int64_t n,
+                                              int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                                              const double* d_warm_start, double* d_ritz_out,
+                                              void* d_ws, size_t ws_bytes, void* d_lanczos,
+                                              size_t lanczos_bytes, void* stream);
+
+/* Synchronise the device and report (and clear) a device-side wait failure. */
+psdgb_status psdgb_check_device_error(void);
+
 /* Lanczos spectral-norm bound (approximate_two_norm): lo and up are host
  * pointers.  The matrix is not modified. */
 psdgb_status psdgb_two_norm(const double* d_A, int64_t n, double* lo, double* up,
@@ -163,7 +186,58 @@ psdgb_status psdgb_project(const char* method, double* d_mat, int64_t n, double*
 psdgb_status psdgb_project_host(const char* method, const double* h_in, double* h_out,
                                 int64_t n, double* h_eigs_out, void* stream);
 
+/* ---- request loop (continuous batching of mixed-size projections) ---------- */
+/* No counterpart in the reference (its calls block and allocate per call).
+ * An ADMM-style caller submits projections of device matrices tagged by a
+ * key (one ADMM stream); the server runs up to max_slots of them at once,
+ * each on its own CUDA stream with private buffers, admits queued requests as
+ * slots and HBM budget free up, keeps each key's last Ritz vector on the
+ * device and warm-starts the key's next Lanczos bound from it, and can replay
+ * one captured CUDA graph per (slot, n).  Requests of one key run in
+ * submission order.  Single host thread. */
+typedef struct psdgb_server psdgb_server;
+
+typedef struct psdgb_server_config {
+    size_t hbm_budget_bytes;  /* device bytes the server may hold (slot buffers, warm starts) */
+    int max_slots;            /* requests in flight at once (1..256) */
+    int precision;            /* psdgb_precision (tensor-core modes) */
+    int schedule;             /* psdgb_schedule */
+    int64_t max_iter;         /* Lanczos steps from the seeded start (reference default 20) */
+    int64_t warm_max_iter;    /* Lanczos steps from a key's previous Ritz vector */
+    int use_graphs;           /* capture each (slot, n) projection once and replay it */
+} psdgb_server_config;
+
+typedef struct psdgb_completion {
+    uint64_t ticket;
+    int64_t key;
+    int64_t n;
+    int status;               /* psdgb_status of the request */
+    double submit_s;          /* psdgb_clock_seconds() at submission */
+    double start_s;           /* ... when the request was admitted to a slot */
+    double end_s;             /* ... when poll saw it finished */
+    double gpu_ms;            /* device time from admission to completion (CUDA events) */
+} psdgb_completion;
+
+double psdgb_clock_seconds(void);
+psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** out);
+psdgb_status psdgb_server_destroy(psdgb_server* server);
+/* Queue the projection of d_in (n x n FP64, device; read when the request
+ * starts) into d_out (device, may equal d_in). */
+psdgb_status psdgb_server_submit(psdgb_server* server, int64_t key, const double* d_in, double* d_out, int64_t n,
+                                 uint64_t* ticket);
+/* Retire finished requests into out[0..cap) (*n_out of them) and admit queued
+ * ones; with wait != 0, block until at least one request finishes. */
+psdgb_status psdgb_server_poll(psdgb_server* server, int wait, psdgb_completion* out, int cap, int* n_out);
+psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queued, size_t* bytes_used,
+                                uint64_t* completed);
+
 /* ---- diagnostics ------------------------------------------------------------ */
+/* Accumulator configuration of the tensor-core products of single-matrix
+ * calls: 0 = four interleaved K accumulators (default), 1 = two accumulators
+ * double-buffered (the epilogue of one tile overlaps the next tile's MMAs),
+ * 2 = one accumulator, four buffers.  Returns the previous value. */
+int psdgb_set_product_config(int acc_mode);
+
 /* Product-kernel timing: when enabled, the library records a CUDA event pair
  * on the caller's stream around every filter-product launch and adds the
  * elapsed times up when the call synchronises.  psdgb_product_timing_read

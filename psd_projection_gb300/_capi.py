@@ -78,6 +78,11 @@ SIGNATURES = {
     "psdgb_release_workspace": (c_int, []),
     "psdgb_composite": (c_int, [c_int, c_int, c_vp, c_i64, c_vp, c_size, c_vp]),
     "psdgb_composite_static": (c_int, [c_int, c_int, c_vp, c_i64, c_vp]),
+    "psdgb_lanczos_state_size": (c_size, [c_i64, c_i64]),
+    "psdgb_composite_auto_scale_async": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_u64, c_int, c_vp, c_vp,
+                                                 c_vp, c_size, c_vp, c_size, c_vp]),
+    "psdgb_check_device_error": (c_int, []),
+    "psdgb_set_product_config": (c_int, [c_int]),
     "psdgb_composite_auto_scale": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_u64, c_int, c_vp, c_size,
                                            c_vp, P_dbl]),
     "psdgb_two_norm": (c_int, [c_vp, c_i64, P_dbl, P_dbl, c_i64, c_dbl, c_u64, c_int, c_vp, c_size, c_vp]),
@@ -97,7 +102,8 @@ SIGNATURES = {
 def header_functions() -> list[str]:
     """Names of every function include/psdgb.h declares."""
     text = HEADER_PATH.read_text()
-    return sorted(set(re.findall(r"\b(psdgb_[a-z0-9_]+)\s*\(", text)))
+    decl = r"(?:psdgb_status|int|size_t|double|uint64_t|const char\s*\*|void)\s+(psdgb_[a-z0-9_]+)\s*\("
+    return sorted(set(re.findall(decl, text)))
 
 
 def lib() -> ctypes.CDLL:

@@ -18,6 +18,9 @@ size_t composite_ws_bytes(int64_t n, int precision);
 psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                            bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
                            void* lz_state, cudaStream_t s, double* up_out);
+psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                               bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out);
 
 namespace {
 
@@ -362,6 +365,39 @@ psdgb_status psdgb_composite_auto_scale(int precision, int schedule, double* d_m
     return finish(ds, s);
 }
 
+size_t psdgb_lanczos_state_size(int64_t n, int64_t max_iter) {
+    if (n <= 0 || max_iter < 0) return 0;
+    return lanczos_state_bytes(n, max_iter);
+}
+
+psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, double* d_mat, int64_t n,
+                                              int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                                              const double* d_warm_start, double* d_ritz_out, void* d_ws,
+                                              size_t ws_bytes, void* d_lanczos, size_t lanczos_bytes, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (n < 0 || max_iter < 0) { set_error("n and max_iter must be >= 0"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n == 0) return PSDGB_OK;
+    if (d_mat == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (d_ws == nullptr || ws_bytes < composite_ws_bytes(n, precision) || d_lanczos == nullptr ||
+        lanczos_bytes < lanczos_state_bytes(n, max_iter)) {
+        set_error("psdgb_composite_auto_scale_async needs caller workspaces of at least "
+                  "psdgb_composite_workspace_size and psdgb_lanczos_state_size bytes");
+        return PSDGB_ERR_WORKSPACE_TOO_SMALL;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    return composite_enqueue(ds, precision, schedule, d_mat, n, d_ws, true, max_iter, tol, seed, residual_mode,
+                             d_lanczos, static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out);
+}
+
+psdgb_status psdgb_check_device_error(void) {
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_CUDA_TRY(cudaDeviceSynchronize());
+    return finish(ds, nullptr);
+}
+
 psdgb_status psdgb_two_norm_ex(const double* d_A, int64_t n, double* lo, double* up, int64_t max_iter, double tol,
                                uint64_t seed, int residual_mode, void* d_ws, size_t ws_bytes, void* stream,
                                double* h_alpha, double* h_beta, int64_t* nb_iter, double* theta) {
@@ -387,8 +423,12 @@ psdgb_status psdgb_two_norm_ex(const double* d_A, int64_t n, double* lo, double*
         void* lz = nullptr;
         PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
         PSDGB_CUDA_TRY(launch_sym_upper_to_f32(d_A, n, static_cast<float*>(a32), ld, s));
-        PSDGB_TRY(lanczos_bound(ds, static_cast<float*>(a32), n, ld, max_iter, tol, seed, residual_mode, lz, s, &lr,
-                                h_alpha, h_beta));
+        PSDGB_TRY(lanczos_bound_async(ds, static_cast<float*>(a32), n, ld, max_iter, tol, seed, residual_mode, lz, s,
+                                      nullptr, nullptr));
+        PSDGB_TRY(lanczos_read(lz, n, max_iter, s, &lr, h_alpha, h_beta));
+    } else {
+        if (h_alpha) for (int64_t i = 0; i < max_iter; ++i) h_alpha[i] = 0.0;
+        if (h_beta) for (int64_t i = 0; i < max_iter; ++i) h_beta[i] = 0.0;
     }
     *lo = lr.lo;
     *up = lr.up;
@@ -461,6 +501,12 @@ psdgb_status psdgb_project_host(const char* method, const double* h_in, double* 
 }
 
 uint64_t psdgb_kernel_launch_count(void) { return g_launches.load(); }
+
+int psdgb_set_product_config(int acc_mode) {
+    const int prev = g_single_acc_mode;
+    if (acc_mode >= ACC_4X1 && acc_mode <= ACC_1X4) g_single_acc_mode = acc_mode;
+    return prev;
+}
 
 psdgb_status psdgb_product_timing_enable(int on) {
     product_timing_collect();

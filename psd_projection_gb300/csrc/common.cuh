@@ -84,7 +84,8 @@ struct EpiParams {
     int np;           // padded dimension (multiple of 128)
     int n;            // true dimension
     float a, b, c;    // EPI_STEP coefficients
-    double up;        // EPI_FINAL scale
+    double up;        // EPI_FINAL scale (times *up_dev when up_dev is set)
+    const double* up_dev;
     SplitMat out;     // EPI_STORE / EPI_STEP destination (may alias A for EPI_STEP)
     SplitMat A;       // EPI_STEP inputs
     SplitMat A3;
@@ -92,6 +93,35 @@ struct EpiParams {
     double* out64;      // EPI_FINAL output (may alias x64)
     int dual;           // mainloop: accumulate P*Q^T + Q*P^T (K doubled), the symmetric part of the product
     float acc_scale;    // the accumulator is multiplied by this first (0.5 for a dual product)
+    int ld;             // row stride of the split-matrix layout (elements); np for a single matrix
+};
+
+// A group of independent blocks sharing one strided operand layout: block b
+// occupies layout rows [row_base, row_base + np) (row stride EpiParams::ld),
+// its FP64 n x n matrix starts at element x_off of the packed input, and its
+// scale (for the final reconstruction) is *up_dev.
+struct BlockDesc {
+    int row_base;
+    int np;
+    int n;
+    int pad;
+    long long x_off;
+    const double* up_dev;
+};
+
+// One 128 x 128 output tile (bi >= bj) of block `block`.
+struct TileDesc {
+    int block;
+    int bi;
+    int bj;
+    int pad;
+};
+
+// The tile list of a grouped product: device tables, or both null for the
+// implicit list of every lower tile of the single block EpiParams describes.
+struct GroupWork {
+    const TileDesc* tiles;
+    const BlockDesc* blocks;
 };
 
 // ---------------------------------------------------------------------------

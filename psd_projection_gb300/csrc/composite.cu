@@ -114,6 +114,7 @@ EpiParams epi_base(const Layout& L, int64_t n) {
     ep.np = static_cast<int>(L.np);
     ep.n = static_cast<int>(n);
     ep.acc_scale = 1.0f;
+    ep.ld = static_cast<int>(L.np);
     return ep;
 }
 
@@ -151,13 +152,15 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
     return PSDGB_OK;
 }
 
-// mat (in place) = (X + up * Xs * A) / 2, Xs = X / up, X read from mat.
-psdgb_status run_final(DeviceState* ds, int precision, const Layout& L, double* mat, int64_t n, double up,
-                       cudaStream_t s) {
-    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0 / up, L.A2, L.fmt, L.np, s));
+// mat (in place) = (X + up * (Xs*A + A*Xs)/2) / 2, Xs = X / up, X read from
+// mat; up is read from the device (up_dev) when given, else 1.
+psdgb_status run_final(DeviceState* ds, int precision, const Layout& L, double* mat, int64_t n, const double* up_dev,
+                       const double* inv_up_dev, cudaStream_t s) {
+    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, inv_up_dev, L.A2, L.fmt, L.np, s));
     EpiParams ef = epi_base(L, n);
     ef.kind = EPI_FINAL;
-    ef.up = up;
+    ef.up = 1.0;
+    ef.up_dev = up_dev;
     // (Xs*A + A*Xs)/2: the symmetric part of the product, as the reference's
     // symmetrisation of W does (src/composite_FP32.cu:153).
     ef.dual = 1;
@@ -218,9 +221,9 @@ size_t composite_ws_bytes(int64_t n, int precision) {
     return 3 * split_matrix_bytes(pi.fmt, pad128(n));
 }
 
-psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
-                           bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
-                           void* lz_state, cudaStream_t s, double* up_out) {
+psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                               bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out) {
     PSDGB_TRY(check_n(n));
     PrecisionInfo pi{};
     if (!precision_info(precision, &pi)) {
@@ -237,23 +240,39 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
         set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (up_out) *up_out = 1.0;
     if (n == 0) return PSDGB_OK;
     const Layout L = make_layout(ws, pi.fmt, n);
-    double up = 1.0;
+    const double* up_dev = nullptr;
+    const double* inv_up_dev = nullptr;
     if (auto_scale) {
+        // The bound runs on the device and leaves scale = up > 0 ? up : 1
+        // (src/composite_FP32.cu:182) and its inverse in the Lanczos state,
+        // which the split kernels and the final epilogue read: no host round trip.
         PSDGB_CUDA_TRY(launch_sym_upper_to_f32(mat, n, L.a32, L.ld, s));
-        LanczosResult lr;
-        PSDGB_TRY(lanczos_bound(ds, L.a32, n, L.ld, max_iter, tol, seed, residual_mode, lz_state, s, &lr, nullptr,
-                                nullptr));
-        up = lr.up > 0.0 ? lr.up : 1.0;  // src/composite_FP32.cu:182
-        PSDGB_CUDA_TRY(launch_split_from_f32(L.a32, n, L.ld, 1.0 / up, L.A, L.fmt, L.np, s));
+        PSDGB_TRY(lanczos_bound_async(ds, L.a32, n, L.ld, max_iter, tol, seed, residual_mode, lz_state, s, d_warm,
+                                      d_ritz_out));
+        up_dev = lanczos_scale_ptr(lz_state, n, max_iter);
+        inv_up_dev = lanczos_inv_scale_ptr(lz_state, n, max_iter);
+        PSDGB_CUDA_TRY(launch_split_from_f32(L.a32, n, L.ld, 1.0, inv_up_dev, L.A, L.fmt, L.np, s));
     } else {
-        PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, L.A, L.fmt, L.np, s));
+        PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, nullptr, L.A, L.fmt, L.np, s));
     }
     PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s));
-    PSDGB_TRY(run_final(ds, precision, L, mat, n, up, s));
-    if (up_out) *up_out = up;
+    PSDGB_TRY(run_final(ds, precision, L, mat, n, up_dev, inv_up_dev, s));
+    return PSDGB_OK;
+}
+
+psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                           bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                           void* lz_state, cudaStream_t s, double* up_out) {
+    if (up_out) *up_out = 1.0;
+    PSDGB_TRY(composite_enqueue(ds, precision, schedule, mat, n, ws, auto_scale, max_iter, tol, seed, residual_mode,
+                                lz_state, s, nullptr, nullptr));
+    if (up_out && auto_scale && n > 0) {
+        LanczosResult lr;
+        PSDGB_TRY(lanczos_read(lz_state, n, max_iter, s, &lr, nullptr, nullptr));
+        *up_out = lr.up > 0.0 ? lr.up : 1.0;
+    }
     return PSDGB_OK;
 }
 

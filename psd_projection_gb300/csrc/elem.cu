@@ -21,8 +21,9 @@ constexpr int TR = 8;   // rows per thread pass
 // result; the input is read coalesced through a shared-memory transpose.
 template <class Store>
 __global__ void sym_upper_tiles(const double* __restrict__ x, int64_t n, int64_t rows_out, int64_t cols_out,
-                                double scale, Store st) {
+                                double scale, const double* scale_dev, Store st) {
     __shared__ double sm[TS][TS + 1];
+    if (scale_dev != nullptr) scale *= *scale_dev;
     const int64_t bi = blockIdx.y, bj = blockIdx.x;
     const int tx = threadIdx.x, ty0 = threadIdx.y;
     // Source block: columns (c) of the column-major input are the tile's j
@@ -65,8 +66,9 @@ struct StoreSplit {
     }
 };
 
-__global__ void split_from_f32_kernel(const float* __restrict__ a, int64_t n, int64_t ld, float scale, SplitMat out,
-                                      int fmt, int64_t np) {
+__global__ void split_from_f32_kernel(const float* __restrict__ a, int64_t n, int64_t ld, double scale64,
+                                      const double* scale_dev, SplitMat out, int fmt, int64_t np) {
+    const float scale = static_cast<float>(scale_dev != nullptr ? scale64 * *scale_dev : scale64);
     const int64_t total = np * np;
     for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < total;
          idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -138,22 +140,22 @@ inline unsigned grid_for(int64_t count, int threads) {
 cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     dim3 block(TS, TR), grid(static_cast<unsigned>((ld + TS - 1) / TS), static_cast<unsigned>((n + TS - 1) / TS));
-    sym_upper_tiles<StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, StoreF32{a32, ld});
+    sym_upper_tiles<StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const SplitMat& out,
-                                  int fmt, int64_t np, cudaStream_t s) {
-    split_from_f32_kernel<<<grid_for(np * np, 256), 256, 0, s>>>(a32, n, ld, static_cast<float>(scale), out, fmt, np);
+cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const double* scale_dev,
+                                  const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
+    split_from_f32_kernel<<<grid_for(np * np, 256), 256, 0, s>>>(a32, n, ld, scale, scale_dev, out, fmt, np);
     count_launch();
     return cudaGetLastError();
 }
 
-cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const SplitMat& out, int fmt,
-                                        int64_t np, cudaStream_t s) {
+cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const double* scale_dev,
+                                        const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
     dim3 block(TS, TR), grid(static_cast<unsigned>((np + TS - 1) / TS), static_cast<unsigned>((np + TS - 1) / TS));
-    sym_upper_tiles<StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, StoreSplit{out, fmt, np});
+    sym_upper_tiles<StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev, StoreSplit{out, fmt, np});
     count_launch();
     return cudaGetLastError();
 }

@@ -31,7 +31,8 @@ __device__ __forceinline__ void epi_element(const EpiParams& ep, int64_t p, int6
     if (ep.kind == EPI_FINAL) {
         if (p < ep.n) {
             const int64_t n = ep.n;
-            const double v = 0.5 * (ep.x64[p * n + q] + ep.up * static_cast<double>(ep.acc_scale * acc));
+            const double up = ep.up_dev ? ep.up * *ep.up_dev : ep.up;
+            const double v = 0.5 * (ep.x64[p * n + q] + up * static_cast<double>(ep.acc_scale * acc));
             ep.out64[p * n + q] = v;
             if (p != q) ep.out64[q * n + p] = v;
         }

@@ -6,18 +6,29 @@
 // two symmetric, commuting matrices is computed on the 128x128 tiles (bi, bj)
 // with bi >= bj only, so half the MMA work of a full GEMM.
 //
-// Kernel structure (one output tile per CTA, 192 threads):
+// One persistent kernel serves a single matrix and a group of independent
+// blocks (a block-diagonal iterate) alike: the operands of every block live
+// in one strided row-major layout (row stride ld), block b occupying rows
+// [row_base_b, row_base_b + np_b); one TMA descriptor per operand term plane
+// covers all blocks.  The work is a list of tiles (block, bi, bj) — implicit
+// (all lower tiles of one block) or a device table — walked round-robin by
+// gridDim.x CTAs, one per SM.
+//
+// CTA structure (192 threads):
 //   warp 0 lane 0  TMA producer: per 64-wide K block, loads the operand term
-//                  tiles of P (rows of tile bi) and Q (rows of tile bj) into a
-//                  STAGES-deep shared-memory ring (128-byte swizzle, K-major);
+//                  tiles of P (rows bi) and Q (rows bj) into a STAGES-deep
+//                  shared-memory ring (128-byte swizzle, K-major), running
+//                  ahead across tile boundaries;
 //   warp 1 lane 0  MMA issuer: tcgen05.mma kind::f16 (FP16 or BF16 in, FP32
 //                  accumulate in TMEM), one MMA per term product per 16-wide
-//                  K slice; tcgen05.commit frees ring stages and signals the
-//                  accumulator;
-//   warps 2-5      epilogue: tcgen05.ld of the 128x128 FP32 accumulator (one
-//                  TMEM lane per tile row), the polynomial step / ReLU
+//                  K slice; the K blocks of a tile are dealt round-robin to
+//                  ACC_SPLIT accumulators (each sees K/ACC_SPLIT additions);
+//                  ACC_BUFS accumulator sets let the next tile's MMAs run while
+//                  the epilogue drains the previous one;
+//   warps 2-5      epilogue: tcgen05.ld of the accumulators (one TMEM lane per
+//                  tile row), their FP32 sum, the polynomial step / ReLU
 //                  reconstruction, operand splitting, and the stores at (p, q)
-//                  and at the mirror (q, p).
+//                  and at the mirror (q, p); then it frees the accumulator set.
 // Because P and Q are symmetric, the B operand "Q^T" is Q itself, so both
 // operands are K-major row blocks of row-major matrices.
 //
@@ -42,19 +53,12 @@ namespace {
 constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int TILE_BYTES = BM * BK * 2;  // one operand term tile: 128 rows x 128 bytes
 constexpr int THREADS = 192;
-// K blocks are dealt round-robin to NACC accumulators of 128 FP32 columns
-// each; the epilogue adds them in FP32 with round-to-nearest.  One tensor-core
-// accumulator summing all of K = 8192 lost accuracy (rel. error 4e-5 against
-// 1e-5 for FP32 FMA at n = 8192, for every operand split, exact BF16x9
-// products included); each of four accumulators sees K/4.
-constexpr int NACC = 4;
-constexpr uint32_t TMEM_COLS = 128 * NACC;
 
 template <int TERMS>
 struct TcCfg {
     static constexpr int STAGES = TERMS == 1 ? 6 : (TERMS == 2 ? 3 : 2);
     static constexpr int STAGE_BYTES = 2 * TERMS * TILE_BYTES;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 512 /*barriers*/;
 };
 
 struct alignas(64) TmapSet {
@@ -80,6 +84,32 @@ __device__ __forceinline__ void tri_decode(int64_t t, int64_t& bi, int64_t& bj) 
     bj = t - i * (i + 1) / 2;
 }
 
+struct TileInfo {
+    int64_t bi, bj;
+    BlockDesc blk;
+};
+
+// Tile t of the work list: from the device tables, or (tables == null) the
+// lower tiles of one block described by the epilogue parameters.
+__device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiParams& ep, int t) {
+    TileInfo ti;
+    if (gw.tiles != nullptr) {
+        const TileDesc td = gw.tiles[t];
+        ti.bi = td.bi;
+        ti.bj = td.bj;
+        ti.blk = gw.blocks[td.block];
+    } else {
+        tri_decode(t, ti.bi, ti.bj);
+        ti.blk.row_base = 0;
+        ti.blk.np = ep.np;
+        ti.blk.n = ep.n;
+        ti.blk.pad = 0;
+        ti.blk.x_off = 0;
+        ti.blk.up_dev = ep.up_dev;
+    }
+    return ti;
+}
+
 __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag, int code) {
     *abort_flag = 1;
     atomicCAS(err, 0, code);
@@ -87,13 +117,14 @@ __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag,
 
 // ---- epilogue helpers ------------------------------------------------------
 
-// Store 32 consecutive values of row p (columns q0..q0+31) and their mirrors.
-// full: every element of the run satisfies p > q (no diagonal masking).
+// Store 32 consecutive values of local row p (columns q0..q0+31) of a block
+// whose first layout row is rb, and their mirrors.  full: every element of
+// the run satisfies p > q (no diagonal masking).
 template <int FMT>
-__device__ __forceinline__ void store_run(const SplitMat& m, int64_t np, int64_t p, int64_t q0, const float (&v)[32],
-                                          bool full) {
+__device__ __forceinline__ void store_run(const SplitMat& m, int64_t ld, int64_t rb, int64_t p, int64_t q0,
+                                          const float (&v)[32], bool full) {
     constexpr int NT = FMT == FMT_F16 ? 2 : 3;
-    const size_t row_idx = static_cast<size_t>(p) * np + q0;
+    const size_t row_idx = static_cast<size_t>(rb + p) * ld + q0;
     if (full) {
         // Direct row store: 32 elements x 2 bytes per term = four 16-byte vectors.
 #pragma unroll
@@ -128,14 +159,14 @@ __device__ __forceinline__ void store_run(const SplitMat& m, int64_t np, int64_t
                 dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
         }
 #pragma unroll
-        for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(q0 + j) * np + p, v[j]);
+        for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(rb + q0 + j) * ld + p, v[j]);
     } else {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
             const int64_t q = q0 + j;
             if (p >= q) {
                 split_store(m, FMT, row_idx + j, v[j]);
-                if (p != q) split_store(m, FMT, static_cast<size_t>(q) * np + p, v[j]);
+                if (p != q) split_store(m, FMT, static_cast<size_t>(rb + q) * ld + p, v[j]);
             }
         }
     }
@@ -172,36 +203,43 @@ __device__ __forceinline__ void load_run(const SplitMat& m, size_t idx, float (&
     }
 }
 
-template <int FMT>
-__device__ void epilogue_tile(const EpiParams& ep, uint32_t tmem_row, int64_t p, int64_t bj, int nacc) {
-    const int64_t np = ep.np;
+// Epilogue of one tile for the thread that owns local row p (tile rows bi).
+template <int FMT, int ACC_SPLIT>
+__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p, int nacc) {
+    const int64_t ld = ep.ld;
+    const int64_t rb = ti.blk.row_base;
     for (int c0 = 0; c0 < BN; c0 += 32) {
         float v[32];
         tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
-        for (int a = 1; a < nacc; ++a) {
-            float w[32];
-            tmem_ld_32cols(tmem_row + static_cast<uint32_t>(a * BN + c0), w);
 #pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] += w[j];
+        for (int a = 1; a < ACC_SPLIT; ++a) {
+            if (a < nacc) {
+                float w[32];
+                tmem_ld_32cols(tmem_row + static_cast<uint32_t>(a * BN + c0), w);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] += w[j];
+            }
         }
-        const int64_t q0 = bj * BN + c0;
+        const int64_t q0 = ti.bj * BN + c0;
         if (q0 > p) continue;  // whole run above the diagonal: owned by the mirror tile
         if (ep.kind == EPI_FINAL) {
-            if (p >= ep.n) continue;
-            const int64_t n = ep.n;
+            const int64_t n = ti.blk.n;
+            if (p >= n) continue;
+            const double up = ti.blk.up_dev ? ep.up * *ti.blk.up_dev : ep.up;
+            double* out = ep.out64 + ti.blk.x_off;
+            const double* x = ep.x64 + ti.blk.x_off;
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
                 const int64_t q = q0 + j;
                 if (q <= p && q < n) {
-                    const double x = ep.x64[p * n + q];
-                    const double o = 0.5 * (x + ep.up * static_cast<double>(ep.acc_scale * v[j]));
-                    ep.out64[p * n + q] = o;
-                    if (q != p) ep.out64[q * n + p] = o;
+                    const double o = 0.5 * (x[p * n + q] + up * static_cast<double>(ep.acc_scale * v[j]));
+                    out[p * n + q] = o;
+                    if (q != p) out[q * n + p] = o;
                 }
             }
             continue;
         }
-        const size_t idx = static_cast<size_t>(p) * np + q0;
+        const size_t idx = static_cast<size_t>(rb + p) * ld + q0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
         if (ep.kind == EPI_STEP) {
@@ -211,43 +249,47 @@ __device__ void epilogue_tile(const EpiParams& ep, uint32_t tmem_row, int64_t p,
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] = fmaf(ep.c, v[j], fmaf(ep.b, a3[j], ep.a * a[j]));
         }
-        store_run<FMT>(ep.out, np, p, q0, v, p > q0 + 31);
+        store_run<FMT>(ep.out, ld, rb, p, q0, v, p > q0 + 31);
     }
 }
 
 // ---- the kernel --------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS>
 __global__ void __launch_bounds__(THREADS, 1)
-    tc_sym_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, int num_kb, int* err) {
+    tc_group_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, const GroupWork gw, int num_tiles,
+                    int* err) {
     using Cfg = TcCfg<TERMS>;
     constexpr int STAGES = Cfg::STAGES;
     constexpr int STAGE_BYTES = Cfg::STAGE_BYTES;
     constexpr uint32_t IDESC = idesc_f16(BM, BN, BF16);
+    constexpr uint32_t TMEM_COLS = ACC_SPLIT * ACC_BUFS * BN;
+    static_assert(TMEM_COLS == 128 || TMEM_COLS == 256 || TMEM_COLS == 512, "TMEM allocation");
 
     extern __shared__ uint8_t smem_raw[];
     const uint32_t raw_addr = smem_u32(smem_raw);
     uint8_t* smem = smem_raw + ((1024u - (raw_addr & 1023u)) & 1023u);
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
     uint64_t* empty = full + STAGES;
-    uint64_t* accf = empty + STAGES;
-    uint64_t* drain = accf + 1;
+    uint64_t* acc_full = empty + STAGES;
+    uint64_t* acc_empty = acc_full + ACC_BUFS;
+    uint64_t* drain = acc_empty + ACC_BUFS;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     volatile int* issued_slot = abort_flag + 1;
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    int64_t bi, bj;
-    tri_decode(blockIdx.x, bi, bj);
-    const int num_kb_half = num_kb;          // K blocks of one product
-    if (ep.dual) num_kb = 2 * num_kb;        // K blocks of the whole mainloop
+    const int dual_mult = ep.dual ? 2 : 1;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(accf, 1);
+        for (int b = 0; b < ACC_BUFS; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+        }
         mbar_init(drain, 1);
         *abort_flag = 0;
         *issued_slot = 0;
@@ -268,73 +310,112 @@ __global__ void __launch_bounds__(THREADS, 1)
             tma_prefetch_desc(&tm.P[t]);
             tma_prefetch_desc(&tm.Q[t]);
         }
-        int issued = 0;
-        for (int kb = 0; kb < num_kb; ++kb) {
-            const int s = kb % STAGES;
-            const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
-            if (!mbar_wait_bounded(&empty[s], ph ^ 1u)) {
-                record_error(err, abort_flag, DEVERR_TMA_WAIT);
-                break;
+        int g = 0;  // K blocks issued by this CTA (ring position)
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x) {
+            const TileInfo ti = tile_info(gw, ep, tile);
+            const int kb_half = ti.blk.np / BK;
+            const int kb_total = kb_half * dual_mult;
+            const int row_p = static_cast<int>(ti.blk.row_base + ti.bi * BM);
+            const int row_q = static_cast<int>(ti.blk.row_base + ti.bj * BN);
+            for (int kb = 0; kb < kb_total; ++kb, ++g) {
+                const int s = g % STAGES;
+                const uint32_t ph = static_cast<uint32_t>(g / STAGES) & 1u;
+                if (!mbar_wait_bounded(&empty[s], ph ^ 1u)) {
+                    record_error(err, abort_flag, DEVERR_TMA_WAIT);
+                    stop = true;
+                    break;
+                }
+                if (*abort_flag) {
+                    stop = true;
+                    break;
+                }
+                uint8_t* st = smem + s * STAGE_BYTES;
+                // In a dual product the second half of the K loop multiplies Q's
+                // rows bi by P's rows bj (the transpose-side term Q * P^T).
+                const bool second = kb >= kb_half;
+                const CUtensorMap* mp = second ? tm.Q : tm.P;
+                const CUtensorMap* mq = second ? tm.P : tm.Q;
+                const int kx = (second ? kb - kb_half : kb) * BK;
+                mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+#pragma unroll
+                for (int t = 0; t < TERMS; ++t) tma_load_2d(st + t * TILE_BYTES, &mp[t], &full[s], kx, row_p);
+#pragma unroll
+                for (int t = 0; t < TERMS; ++t)
+                    tma_load_2d(st + (TERMS + t) * TILE_BYTES, &mq[t], &full[s], kx, row_q);
+                *issued_slot = g + 1;
             }
-            if (*abort_flag) break;
-            uint8_t* st = smem + s * STAGE_BYTES;
-            // In a dual product the second half of the K loop multiplies Q's
-            // rows bi by P's rows bj (the transpose-side term Q * P^T).
-            const bool second = kb >= num_kb_half;
-            const CUtensorMap* mp = second ? tm.Q : tm.P;
-            const CUtensorMap* mq = second ? tm.P : tm.Q;
-            const int kx = (second ? kb - num_kb_half : kb) * BK;
-            mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-#pragma unroll
-            for (int t = 0; t < TERMS; ++t)
-                tma_load_2d(st + t * TILE_BYTES, &mp[t], &full[s], kx, static_cast<int>(bi * BM));
-#pragma unroll
-            for (int t = 0; t < TERMS; ++t)
-                tma_load_2d(st + (TERMS + t) * TILE_BYTES, &mq[t], &full[s], kx, static_cast<int>(bj * BN));
-            issued = kb + 1;
         }
-        *issued_slot = issued;
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
-        bool ok = true;
-        for (int kb = 0; kb < num_kb; ++kb) {
-            const int s = kb % STAGES;
-            const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
-            if (!mbar_wait_bounded(&full[s], ph)) {
+        int g = 0, it = 0;
+        bool stop = false;
+        for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x, ++it) {
+            const TileInfo ti = tile_info(gw, ep, tile);
+            const int kb_total = (ti.blk.np / BK) * dual_mult;
+            const int buf = it % ACC_BUFS;
+            const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
+            if (!mbar_wait_bounded(&acc_empty[buf], use_ph ^ 1u)) {
                 record_error(err, abort_flag, DEVERR_MMA_WAIT);
-                ok = false;
                 break;
             }
-            if (*abort_flag) { ok = false; break; }
             tc_fence_after();
-            const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
-#pragma unroll
-            for (int k = 0; k < BK / 16; ++k) {
-#pragma unroll
-                for (int pi = 0; pi < NPROD; ++pi) {
-                    const uint64_t ad = sdesc_kmajor_sw128(base + prod_a(pi) * TILE_BYTES + k * 32);
-                    const uint64_t bd = sdesc_kmajor_sw128(base + (TERMS + prod_b(pi)) * TILE_BYTES + k * 32);
-                    umma_f16(tmem + static_cast<uint32_t>((kb % NACC) * BN), ad, bd, IDESC,
-                             (kb >= NACC || k != 0 || pi != 0) ? 1u : 0u);
+            const uint32_t acc_base = tmem + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
+            for (int kb = 0; kb < kb_total; ++kb, ++g) {
+                const int s = g % STAGES;
+                const uint32_t ph = static_cast<uint32_t>(g / STAGES) & 1u;
+                if (!mbar_wait_bounded(&full[s], ph)) {
+                    record_error(err, abort_flag, DEVERR_MMA_WAIT);
+                    stop = true;
+                    break;
                 }
+                if (*abort_flag) {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t base = smem_u32(smem + s * STAGE_BYTES);
+                const uint32_t acc = acc_base + static_cast<uint32_t>((kb % ACC_SPLIT) * BN);
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+#pragma unroll
+                    for (int pi = 0; pi < NPROD; ++pi) {
+                        const uint64_t ad = sdesc_kmajor_sw128(base + prod_a(pi) * TILE_BYTES + k * 32);
+                        const uint64_t bd = sdesc_kmajor_sw128(base + (TERMS + prod_b(pi)) * TILE_BYTES + k * 32);
+                        umma_f16(acc, ad, bd, IDESC, (kb >= ACC_SPLIT || k != 0 || pi != 0) ? 1u : 0u);
+                    }
+                }
+                umma_commit(&empty[s]);
             }
-            umma_commit(&empty[s]);
+            if (stop) break;
+            umma_commit(&acc_full[buf]);
         }
-        if (ok) umma_commit(accf);
     } else if (warp >= 2) {
         // ---- epilogue ----
         const int q4 = warp & 3;  // TMEM lane quarter this warp may access
-        const int64_t p = bi * BM + q4 * 32 + lane;
-        if (!mbar_wait_bounded(accf, 0)) {
-            record_error(err, abort_flag, DEVERR_EPI_WAIT);
-        } else if (!*abort_flag) {
+        int it = 0;
+        for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
+            const TileInfo ti = tile_info(gw, ep, tile);
+            const int kb_total = (ti.blk.np / BK) * dual_mult;
+            const int buf = it % ACC_BUFS;
+            const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
+            if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {
+                record_error(err, abort_flag, DEVERR_EPI_WAIT);
+                break;
+            }
+            if (*abort_flag) break;
             tc_fence_after();
-            const uint32_t tmem_row = tmem + (static_cast<uint32_t>(q4 * 32) << 16);
-            const int nacc = num_kb < NACC ? num_kb : NACC;
+            const int64_t p = ti.bi * BM + q4 * 32 + lane;
+            const uint32_t tmem_row =
+                tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
+            const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
             if (ep.fmt == FMT_F16)
-                epilogue_tile<FMT_F16>(ep, tmem_row, p, bj, nacc);
+                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p, nacc);
             else
-                epilogue_tile<FMT_BF16>(ep, tmem_row, p, bj, nacc);
+                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p, nacc);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[buf]);
         }
     }
 
@@ -350,10 +431,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         if (warp == 0 && lane == 0) {
             // Wait for the loads of the last STAGES issued K blocks to land.
             const int issued = *issued_slot;
-            for (int kb = issued - STAGES; kb < issued; ++kb) {
-                if (kb < 0) continue;
-                const int s = kb % STAGES;
-                const uint32_t ph = static_cast<uint32_t>(kb / STAGES) & 1u;
+            for (int g = issued - STAGES; g < issued; ++g) {
+                if (g < 0) continue;
+                const int s = g % STAGES;
+                const uint32_t ph = static_cast<uint32_t>(g / STAGES) & 1u;
                 if (!mbar_wait_bounded(&full[s], ph)) atomicCAS(err, 0, DEVERR_DRAIN_WAIT);
             }
         }
@@ -381,11 +462,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-bool make_tmap(CUtensorMap* tm, void* base, int64_t np, bool bf16) {
+// Tensor map over a row-major plane of `rows` rows with row stride ld (both
+// in elements; the inner extent is ld).
+bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16) {
     auto fn = encode_fn();
     if (!fn) return false;
-    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(np), static_cast<cuuint64_t>(np)};
-    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(np) * 2};
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ld), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
     const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BM)};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r =
@@ -395,50 +478,81 @@ bool make_tmap(CUtensorMap* tm, void* base, int64_t np, bool bf16) {
     return r == CUDA_SUCCESS;
 }
 
-template <int TERMS, int NPROD, bool BF16>
-psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t np, const EpiParams& ep,
-                       cudaStream_t s) {
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS>
+psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
+                       const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
     using Cfg = TcCfg<TERMS>;
+    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS>;
     static bool configured = false;  // attribute set once per process (per instantiation)
     if (!configured) {
-        PSDGB_CUDA_TRY(cudaFuncSetAttribute(tc_sym_kernel<TERMS, NPROD, BF16>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
+        PSDGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
         configured = true;
     }
     TmapSet tm;
     for (int t = 0; t < 3; ++t) {
         void* pb = (t < TERMS) ? P.term[t] : P.term[0];
         void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
-        if (!make_tmap(&tm.P[t], pb, np, BF16) || !make_tmap(&tm.Q[t], qb, np, BF16)) {
+        if (!make_tmap(&tm.P[t], pb, ld, rows, BF16) || !make_tmap(&tm.Q[t], qb, ld, rows, BF16)) {
             set_error("cuTensorMapEncodeTiled failed");
             return PSDGB_ERR_CUDA;
         }
     }
-    const int64_t nt = np / BM;
-    const int64_t tiles = nt * (nt + 1) / 2;
-    const int num_kb = static_cast<int>(np / BK);
-    tc_sym_kernel<TERMS, NPROD, BF16>
-        <<<static_cast<unsigned>(tiles), THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, num_kb, ds->d_error);
+    if (num_tiles <= 0) return PSDGB_OK;
+    int g = grid > 0 ? grid : ds->sm_count;
+    if (g > num_tiles) g = static_cast<int>(num_tiles);
+    kern<<<static_cast<unsigned>(g), THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, gw, static_cast<int>(num_tiles),
+                                                                    ds->d_error);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     return PSDGB_OK;
 }
 
+template <int TERMS, int NPROD, bool BF16>
+psdgb_status launch_acc(DeviceState* ds, int acc_mode, const SplitMat& P, const SplitMat& Q, int64_t ld,
+                        int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid,
+                        cudaStream_t s) {
+    switch (acc_mode) {
+        case ACC_4X1: return launch_tc<TERMS, NPROD, BF16, 4, 1>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_2X2: return launch_tc<TERMS, NPROD, BF16, 2, 2>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_1X4: return launch_tc<TERMS, NPROD, BF16, 1, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        default: break;
+    }
+    set_error("gemm_tc: unknown accumulator mode");
+    return PSDGB_ERR_INVALID_ARGUMENT;
+}
+
 }  // namespace
 
-psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
-                     const EpiParams& ep, cudaStream_t s) {
+psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
+                           int64_t ld, int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles,
+                           int grid, cudaStream_t s) {
     switch (precision) {
-        case PSDGB_PREC_FP16: return launch_tc<1, 1, false>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16: return launch_tc<1, 1, true>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_FP16X3: return launch_tc<2, 3, false>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X3: return launch_tc<2, 3, true>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X6: return launch_tc<3, 6, true>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X9: return launch_tc<3, 9, true>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_FP16: return launch_acc<1, 1, false>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_BF16: return launch_acc<1, 1, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_FP16X3:
+            return launch_acc<2, 3, false>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_BF16X3:
+            return launch_acc<2, 3, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_BF16X6:
+            return launch_acc<3, 6, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_BF16X9:
+            return launch_acc<3, 9, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         default: break;
     }
     set_error("gemm_tc: unknown precision");
     return PSDGB_ERR_INVALID_ARGUMENT;
 }
+
+// One matrix: the implicit tile list of all lower tiles of an np x np operand.
+psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                     const EpiParams& ep, cudaStream_t s) {
+    const int64_t nt = np / BM;
+    GroupWork gw{nullptr, nullptr};
+    EpiParams e = ep;
+    e.ld = static_cast<int>(np);
+    return gemm_tc_group(ds, precision, g_single_acc_mode, P, Q, np, np, e, gw, nt * (nt + 1) / 2, 0, s);
+}
+
+int g_single_acc_mode = ACC_4X1;
 
 }  // namespace psdgb

@@ -65,12 +65,13 @@ size_t split_matrix_bytes(int fmt, int64_t np);
 // a32 (n x ld, ld = pad4(n), zero padded) = FP32 of the symmetric matrix
 // defined by the upper triangle of the column-major FP64 matrix x.
 cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s);
-// out (Np x Np split matrix) = split(scale * a32), zero padding.
-cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const SplitMat& out,
-                                  int fmt, int64_t np, cudaStream_t s);
-// out (Np x Np split matrix) = split(scale * sym_upper(x)), zero padding.
-cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const SplitMat& out, int fmt,
-                                        int64_t np, cudaStream_t s);
+// out (Np x Np split matrix) = split(scale * (*scale_dev) * a32), zero padding
+// (scale_dev may be null: factor 1).
+cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const double* scale_dev,
+                                  const SplitMat& out, int fmt, int64_t np, cudaStream_t s);
+// out (Np x Np split matrix) = split(scale * (*scale_dev) * sym_upper(x)), zero padding.
+cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const double* scale_dev,
+                                        const SplitMat& out, int fmt, int64_t np, cudaStream_t s);
 // FP64 reductions: out[0] = sum (a-b)^2, out[1] = sum b^2 over n*n elements.
 cudaError_t launch_diff_norms(const double* a, const double* b, int64_t count, double* d_out2, cudaStream_t s);
 // Scale column j of v (n x n col-major FP64) by max(w[j], 0).
@@ -88,6 +89,16 @@ psdgb_status gemm_simt(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
                        cudaStream_t s);
 psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                      const EpiParams& ep, cudaStream_t s);
+// Accumulator configurations of the tensor-core product kernel: ACC_SPLIT
+// interleaved accumulators (K/ACC_SPLIT additions each) x ACC_BUFS sets
+// (epilogue of one tile overlapping the next tile's MMAs); 512 TMEM columns.
+enum AccMode : int { ACC_4X1 = 0, ACC_2X2 = 1, ACC_1X4 = 2 };
+extern int g_single_acc_mode;  // configuration of the single-matrix products
+// Grouped product over a tile list (see GroupWork), persistent over `grid`
+// CTAs (0: one per SM); operand planes of `rows` rows with row stride ld.
+psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
+                           int64_t ld, int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles,
+                           int grid, cudaStream_t s);
 
 // ---- Lanczos (lanczos.cu) ---------------------------------------------------------
 struct LanczosResult {
@@ -95,14 +106,18 @@ struct LanczosResult {
     int64_t nb_iter = 0;
 };
 size_t lanczos_state_bytes(int64_t n, int64_t max_iter);
-// Runs the bound on a32 (n x ld FP32, symmetric).  h_alpha / h_beta may be null.
-psdgb_status lanczos_bound(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter, double tol,
-                           uint64_t seed, int residual_mode, void* d_state, cudaStream_t s, LanczosResult* res,
-                           double* h_alpha, double* h_beta);
-
-// ---- host tridiagonal solver (tridiag.cpp) ------------------------------------------
-// Largest eigenvalue of the symmetric tridiagonal matrix (diag d[0..m),
-// off-diagonal e[0..m-1)) and a unit eigenvector for it.
-void tridiag_largest_eigenpair(const double* d, const double* e, int64_t m, double* theta, double* vec);
+// Enqueue the whole bound on a32 (n x ld FP32, symmetric) on stream s; the
+// results stay in the device state.  d_warm (n doubles, may be null) replaces
+// the seeded start vector; d_ritz_out (n doubles, may be null) receives the
+// Ritz vector.  No host synchronisation.
+psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter,
+                                 double tol, uint64_t seed, int residual_mode, void* d_state, cudaStream_t s,
+                                 const double* d_warm, double* d_ritz_out);
+// Device addresses of the scale (up, or 1) and of its inverse in the state.
+const double* lanczos_scale_ptr(void* d_state, int64_t n, int64_t max_iter);
+const double* lanczos_inv_scale_ptr(void* d_state, int64_t n, int64_t max_iter);
+// Copy the bound (and alpha/beta when non-null) to the host; synchronises s.
+psdgb_status lanczos_read(void* d_state, int64_t n, int64_t max_iter, cudaStream_t s, LanczosResult* res,
+                          double* h_alpha, double* h_beta);
 
 }  // namespace psdgb

@@ -14,10 +14,14 @@
 // GB300 design: the matrix is streamed as FP32 (4 n^2 bytes per matvec
 // instead of the reference's 8 n^2 per Dgemv, two per step), one warp per
 // column with 128-bit loads and warp-shuffle reductions, FP64 for every
-// reduction and every vector; the recurrence runs on the device (no host
-// round trip per step) and the host reads alpha/beta once at the end.  The
-// start vector comes from a counter-based hash (SplitMix64) of a caller seed
-// instead of the reference's nondeterministic curand seed (src/utils.cu:188-214).
+// reduction and every vector.  The whole bound runs on the device: the
+// recurrence, the largest eigenpair of T (Sturm-sequence multisection in one
+// warp and inverse iteration, instead of the reference's cuSOLVER Dsyevd
+// with host round trips), the Ritz residual, and the scale 1/up the filter
+// consumes — so a projection needs no host synchronisation and can be
+// captured in a CUDA graph.  The start vector comes from a counter-based hash
+// (SplitMix64) of a caller seed instead of the reference's nondeterministic
+// curand seed (src/utils.cu:188-214), or from a caller-supplied warm start.
 #include <cmath>
 #include <vector>
 
@@ -29,14 +33,18 @@ namespace {
 
 struct LzState {
     int nb_iter;
-    int stopped;
+    int stopped;    // the recurrence stopped (skip the remaining steps)
+    int no_ritz;    // nb_iter == 0: skip the Ritz residual
+    int pad;
     double beta_old;
-    double resid_norm2;   // sum of squares of the Ritz residual
+    double resid_norm2;  // sum of squares of the Ritz residual
+    double theta, lo, up;
+    double scale, inv_scale;  // scale = up > 0 ? up : 1 (src/composite_FP32.cu:182)
 };
 
 // Layout of the Lanczos state inside its buffer.
 struct LzLayout {
-    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk;
+    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk, work;
     size_t total;
 };
 
@@ -59,6 +67,7 @@ LzLayout lz_layout(int64_t n, int64_t m) {
     L.q32 = take(sizeof(float) * n4);
     L.u32 = take(sizeof(float) * n4);
     L.uk = take(sizeof(double) * (m + 1));
+    L.work = take(sizeof(double) * 4 * (m + 1));  // tridiagonal LU of the inverse iteration
     L.total = off;
     return L;
 }
@@ -83,14 +92,20 @@ __device__ double block_sum(double v, double* red) {
     return t;
 }
 
-// q = uniform(0,1] from the seed, normalised; V[:,0] = q; q_old = 0.
-__global__ void lz_init_kernel(int64_t n, uint64_t seed, LzState* st, double* q, double* vold, double* V,
-                               float* q32) {
+// q = start vector (uniform(0,1] from the seed, or the warm start), normalised;
+// V[:,0] = q; q_old = 0.
+__global__ void lz_init_kernel(int64_t n, uint64_t seed, const double* __restrict__ warm, LzState* st, double* q,
+                               double* vold, double* V, float* q32) {
     __shared__ double red[32];
     double ss = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-        const uint64_t h = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
-        const double u = static_cast<double>((h >> 11) + 1) * 0x1.0p-53;  // (0, 1]
+        double u;
+        if (warm != nullptr) {
+            u = warm[i];
+        } else {
+            const uint64_t h = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
+            u = static_cast<double>((h >> 11) + 1) * 0x1.0p-53;  // (0, 1]
+        }
         q[i] = u;
         ss += u * u;
     }
@@ -106,19 +121,26 @@ __global__ void lz_init_kernel(int64_t n, uint64_t seed, LzState* st, double* q,
     if (threadIdx.x == 0) {
         st->nb_iter = 0;
         st->stopped = 0;
+        st->no_ritz = 0;
         st->beta_old = 0.0;
         st->resid_norm2 = 0.0;
+        st->theta = 0.0;
+        st->lo = 0.0;
+        st->up = 1.0;
+        st->scale = 1.0;
+        st->inv_scale = 1.0;
     }
 }
 
 // y[c] = sum_r A[c*ld + r] * x[r] for every column c of the symmetric FP32
 // matrix A (so y = A x = A^T x).  One warp per column, float4 loads, FP32
-// partial sums per lane, FP64 across lanes.  x is staged in shared memory.
-// Writes y as FP64 (y64) and/or FP32 (y32).
+// partial sums per lane flushed to FP64 every 64 vectors, FP64 across lanes.
+// x is staged in shared memory.  Writes y as FP64 (y64) and/or FP32 (y32).
+// The whole kernel is skipped when *skip is non-zero.
 __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict__ A, int64_t n, int64_t ld,
                                                         const float* __restrict__ x, double* __restrict__ y64,
-                                                        float* __restrict__ y32, const LzState* st) {
-    if (st != nullptr && st->stopped) return;
+                                                        float* __restrict__ y32, const int* skip) {
+    if (skip != nullptr && *skip) return;
     extern __shared__ float4 xs4[];
     float* xs = reinterpret_cast<float*>(xs4);
     const int64_t ld4 = ld / 4;
@@ -132,7 +154,6 @@ __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict_
         float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
         double acc = 0.0;
         int64_t k = lane;
-        // Flush the FP32 partials into FP64 every 64 float4 per lane.
         while (k < ld4) {
             const int64_t kend = (k + 32 * 64 < ld4) ? k + 32 * 64 : ld4;
             for (; k < kend; k += 32) {
@@ -199,31 +220,190 @@ __global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzStat
     }
 }
 
-// y = V[:, 0:m] u; y32 = FP32(y).
-__global__ void lz_ritz_kernel(int64_t n, int64_t m, const double* __restrict__ V, const double* __restrict__ u,
-                               double* y, float* y32) {
+// ---- the tridiagonal eigenpair, on the device (one thread) ------------------
+
+// Number of eigenvalues of T strictly less than x (Sturm count of the LDL^T
+// pivots of T - x I).
+__device__ int64_t sturm_count(const double* d, const double* e, int64_t m, double x, double pivmin) {
+    int64_t cnt = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0) ++cnt;
+    for (int64_t i = 1; i < m; ++i) {
+        q = d[i] - x - e[i - 1] * e[i - 1] / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        if (q < 0) ++cnt;
+    }
+    return cnt;
+}
+
+// Solve (T - shift I) x = b in place by Gaussian elimination with partial
+// pivoting on the band (fill-in on a second superdiagonal); work holds 4m doubles.
+__device__ void tridiag_solve(const double* d, const double* e, int64_t m, double shift, double tiny, double* b,
+                              double* work) {
+    double* dl = work;
+    double* dd = work + m;
+    double* du = work + 2 * m;
+    double* du2 = work + 3 * m;
+    for (int64_t i = 0; i < m; ++i) {
+        dd[i] = d[i] - shift;
+        dl[i] = (i + 1 < m) ? e[i] : 0.0;
+        du[i] = (i + 1 < m) ? e[i] : 0.0;
+        du2[i] = 0.0;
+    }
+    for (int64_t i = 0; i + 1 < m; ++i) {
+        if (fabs(dd[i]) >= fabs(dl[i])) {
+            if (dd[i] == 0.0) dd[i] = tiny;
+            const double f = dl[i] / dd[i];
+            dd[i + 1] -= f * du[i];
+            b[i + 1] -= f * b[i];
+            dl[i] = 0.0;
+        } else {  // swap rows i and i+1
+            const double f = dd[i] / dl[i];
+            dd[i] = dl[i];
+            const double t = dd[i + 1];
+            dd[i + 1] = du[i] - f * t;
+            du[i] = t;
+            if (i + 2 < m) {
+                du2[i] = du[i + 1];
+                du[i + 1] = -f * du2[i];
+            }
+            const double tb = b[i];
+            b[i] = b[i + 1];
+            b[i + 1] = tb - f * b[i];
+        }
+    }
+    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
+    b[m - 1] /= dd[m - 1];
+    if (m > 1) b[m - 2] = (b[m - 2] - du[m - 2] * b[m - 1]) / dd[m - 2];
+    for (int64_t i = m - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) / dd[i];
+}
+
+// The reference forms T densely and takes the last eigenpair of cuSOLVER
+// Dsyevd (src/lanczos.cu:186-240).  Here one warp: theta by 33-way
+// multisection on the Sturm count (each lane evaluates one split point, a
+// ballot picks the sub-interval; about 11 rounds to full FP64 precision
+// instead of ~50 bisection steps of dependent FP64 divisions), then u by four
+// steps of inverse iteration in lane 0.
+__global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double* beta, double* uk, double* work) {
+    const int lane = threadIdx.x;
+    const int64_t m = st->nb_iter;
+    if (m == 0) {  // the all-zero branch of src/lanczos.cu:171-184
+        if (lane == 0) {
+            st->no_ritz = 1;
+            st->lo = 0.0;
+            st->up = 1.0;
+            st->theta = 0.0;
+            st->scale = 1.0;
+            st->inv_scale = 1.0;
+        }
+        return;
+    }
+    if (m == 1) {
+        if (lane == 0) {
+            st->no_ritz = 0;
+            st->theta = alpha[0];
+            uk[0] = 1.0;
+        }
+        return;
+    }
+    const double* d = alpha;
+    const double* e = beta;
+    double lo = INFINITY, hi = -INFINITY, tnorm = 0.0;
+    for (int64_t i = 0; i < m; ++i) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < m ? fabs(e[i]) : 0.0);
+        lo = fmin(lo, d[i] - r);
+        hi = fmax(hi, d[i] + r);
+        tnorm = fmax(tnorm, fabs(d[i]) + r);
+    }
+    const double eps = 2.220446049250313e-16;
+    const double pivmin = fmax(2.2250738585072014e-308, eps * eps * tnorm * tnorm);
+    const double pad = 2.0 * eps * tnorm + pivmin;
+    lo -= pad;
+    hi += pad;
+    // Invariant: count(lo) < m <= count(hi); the largest eigenvalue lies in [lo, hi).
+    for (int it = 0; it < 64; ++it) {
+        if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
+        const double x = lo + (hi - lo) * (static_cast<double>(lane + 1) / 33.0);
+        const bool above = (x > lo && x < hi) ? (sturm_count(d, e, m, x, pivmin) >= m) : (x >= hi);
+        const unsigned mask = __ballot_sync(0xffffffffu, above);
+        const int first = mask ? __ffs(mask) - 1 : 32;  // first split point with all eigenvalues below it
+        const double new_hi = (first < 32) ? __shfl_sync(0xffffffffu, x, first) : hi;
+        const double new_lo = (first > 0) ? __shfl_sync(0xffffffffu, x, first > 0 ? first - 1 : 0) : lo;
+        if (!(new_hi < hi || new_lo > lo)) break;  // no progress at this precision
+        hi = new_hi;
+        lo = new_lo;
+    }
+    if (lane != 0) return;
+    st->no_ritz = 0;
+    const double t = 0.5 * (lo + hi);
+    st->theta = t;
+    const double tiny = eps * fmax(tnorm, 2.2250738585072014e-308);
+    const double shift = t + 4.0 * eps * fmax(tnorm, fabs(t));
+    for (int64_t i = 0; i < m; ++i) uk[i] = 1.0;
+    for (int it = 0; it < 4; ++it) {
+        tridiag_solve(d, e, m, shift, tiny, uk, work);
+        double s = 0.0;
+        for (int64_t i = 0; i < m; ++i) s += uk[i] * uk[i];
+        s = sqrt(s);
+        if (!(s > 0.0) || !isfinite(s)) {
+            for (int64_t i = 0; i < m; ++i) uk[i] = 1.0 / sqrt(static_cast<double>(m));
+            break;
+        }
+        for (int64_t i = 0; i < m; ++i) uk[i] /= s;
+    }
+}
+
+// y = V[:, 0:m] u (m = nb_iter); y32 = FP32(y); optionally the Ritz vector out.
+__global__ void lz_ritz_kernel(int64_t n, const LzState* st, const double* __restrict__ V,
+                               const double* __restrict__ u, double* y, float* y32, double* ritz_out) {
+    if (st->no_ritz) return;
+    const int64_t m = st->nb_iter;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double s = 0.0;
         for (int64_t j = 0; j < m; ++j) s += V[j * n + i] * u[j];
         y[i] = s;
         y32[i] = static_cast<float>(s);
+        if (ritz_out) ritz_out[i] = s;
     }
 }
 
-// resid_norm2 = ||ry - theta y||^2 (single block).
-__global__ void lz_resid_kernel(int64_t n, double theta, const double* ry, const double* y, LzState* st) {
+// ||ry - theta y|| and the bound: lo = sqrt(theta), up = sqrt(theta + ||r||),
+// scale = up > 0 ? up : 1 (single block).
+__global__ void lz_resid_kernel(int64_t n, const double* ry, const double* y, LzState* st) {
+    if (st->no_ritz) return;
     __shared__ double red[32];
+    const double theta = st->theta;
     double s = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const double r = ry[i] - theta * y[i];
         s += r * r;
     }
     const double t = block_sum(s, red);
-    if (threadIdx.x == 0) st->resid_norm2 = t;
+    if (threadIdx.x == 0) {
+        st->resid_norm2 = t;
+        const double up = sqrt(theta + sqrt(t));
+        st->lo = sqrt(theta);
+        st->up = up;
+        const double scale = up > 0.0 ? up : 1.0;
+        st->scale = scale;
+        st->inv_scale = 1.0 / scale;
+    }
 }
 
-cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double* y64, float* y32, const LzState* st,
+// No iteration at all (max_iter or n is 0): lo = 0, up = 1.
+__global__ void lz_trivial_kernel(LzState* st) {
+    st->nb_iter = 0;
+    st->no_ritz = 1;
+    st->theta = 0.0;
+    st->lo = 0.0;
+    st->up = 1.0;
+    st->scale = 1.0;
+    st->inv_scale = 1.0;
+}
+
+cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double* y64, float* y32, const int* skip,
                    int sm_count, cudaStream_t s) {
     const size_t smem = sizeof(float) * static_cast<size_t>(ld);
     const int threads = 256;
@@ -231,28 +411,63 @@ cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double
     const int64_t cap = static_cast<int64_t>(sm_count) * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    lz_matvec_kernel<<<static_cast<unsigned>(blocks), threads, smem, s>>>(A, n, ld, x, y64, y32, st);
+    lz_matvec_kernel<<<static_cast<unsigned>(blocks), threads, smem, s>>>(A, n, ld, x, y64, y32, skip);
     count_launch();
     return cudaGetLastError();
+}
+
+struct LzPtrs {
+    LzState* st;
+    double *alpha, *beta, *q, *w, *vold, *V, *y, *ry, *uk, *work;
+    float *q32, *u32;
+};
+
+LzPtrs lz_ptrs(void* d_state, int64_t n, int64_t m) {
+    const LzLayout L = lz_layout(n, m);
+    char* base = static_cast<char*>(d_state);
+    LzPtrs p;
+    p.st = reinterpret_cast<LzState*>(base + L.state);
+    p.alpha = reinterpret_cast<double*>(base + L.alpha);
+    p.beta = reinterpret_cast<double*>(base + L.beta);
+    p.q = reinterpret_cast<double*>(base + L.q);
+    p.w = reinterpret_cast<double*>(base + L.w);
+    p.vold = reinterpret_cast<double*>(base + L.vold);
+    p.V = reinterpret_cast<double*>(base + L.V);
+    p.y = reinterpret_cast<double*>(base + L.y);
+    p.ry = reinterpret_cast<double*>(base + L.ry);
+    p.q32 = reinterpret_cast<float*>(base + L.q32);
+    p.u32 = reinterpret_cast<float*>(base + L.u32);
+    p.uk = reinterpret_cast<double*>(base + L.uk);
+    p.work = reinterpret_cast<double*>(base + L.work);
+    return p;
 }
 
 }  // namespace
 
 size_t lanczos_state_bytes(int64_t n, int64_t max_iter) {
     const int64_t m = max_iter < n ? max_iter : n;
-    return lz_layout(n, m).total;
+    return lz_layout(n, m < 0 ? 0 : m).total;
 }
 
-psdgb_status lanczos_bound(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter, double tol,
-                           uint64_t seed, int residual_mode, void* d_state, cudaStream_t s, LanczosResult* res,
-                           double* h_alpha, double* h_beta) {
+const double* lanczos_scale_ptr(void* d_state, int64_t n, int64_t max_iter) {
+    const int64_t m = max_iter < n ? max_iter : n;
+    return &lz_ptrs(d_state, n, m < 0 ? 0 : m).st->scale;
+}
+
+const double* lanczos_inv_scale_ptr(void* d_state, int64_t n, int64_t max_iter) {
+    const int64_t m = max_iter < n ? max_iter : n;
+    return &lz_ptrs(d_state, n, m < 0 ? 0 : m).st->inv_scale;
+}
+
+psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, int64_t ld, int64_t max_iter,
+                                 double tol, uint64_t seed, int residual_mode, void* d_state, cudaStream_t s,
+                                 const double* d_warm, double* d_ritz_out) {
     const int64_t m = max_iter < n ? max_iter : n;  // src/lanczos.cu:55
-    *res = LanczosResult{};
-    if (h_alpha) for (int64_t i = 0; i < max_iter; ++i) h_alpha[i] = 0.0;
-    if (h_beta) for (int64_t i = 0; i < max_iter; ++i) h_beta[i] = 0.0;
+    const LzPtrs P = lz_ptrs(d_state, n, m < 0 ? 0 : m);
     if (m <= 0) {  // no iteration: the all-zero branch of src/lanczos.cu:171-184
-        res->lo = 0.0;
-        res->up = 1.0;
+        lz_trivial_kernel<<<1, 1, 0, s>>>(P.st);
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
         return PSDGB_OK;
     }
     const size_t xs_bytes = sizeof(float) * static_cast<size_t>(ld);
@@ -264,77 +479,63 @@ psdgb_status lanczos_bound(DeviceState* ds, const float* a32, int64_t n, int64_t
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_matvec_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             static_cast<int>(xs_bytes)));
     }
-    const LzLayout L = lz_layout(n, m);
-    char* base = static_cast<char*>(d_state);
-    LzState* st = reinterpret_cast<LzState*>(base + L.state);
-    double* alpha = reinterpret_cast<double*>(base + L.alpha);
-    double* beta = reinterpret_cast<double*>(base + L.beta);
-    double* q = reinterpret_cast<double*>(base + L.q);
-    double* w = reinterpret_cast<double*>(base + L.w);
-    double* vold = reinterpret_cast<double*>(base + L.vold);
-    double* V = reinterpret_cast<double*>(base + L.V);
-    double* y = reinterpret_cast<double*>(base + L.y);
-    double* ry = reinterpret_cast<double*>(base + L.ry);
-    float* q32 = reinterpret_cast<float*>(base + L.q32);
-    float* u32 = reinterpret_cast<float*>(base + L.u32);
-    double* uk = reinterpret_cast<double*>(base + L.uk);
-
-    PSDGB_CUDA_TRY(cudaMemsetAsync(alpha, 0, sizeof(double) * (m + 1), s));
-    PSDGB_CUDA_TRY(cudaMemsetAsync(beta, 0, sizeof(double) * (m + 1), s));
-    lz_init_kernel<<<1, 1024, 0, s>>>(n, seed, st, q, vold, V, q32);
+    PSDGB_CUDA_TRY(cudaMemsetAsync(P.alpha, 0, sizeof(double) * (m + 1), s));
+    PSDGB_CUDA_TRY(cudaMemsetAsync(P.beta, 0, sizeof(double) * (m + 1), s));
+    lz_init_kernel<<<1, 1024, 0, s>>>(n, seed, d_warm, P.st, P.q, P.vold, P.V, P.q32);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
 
+    const int* stopped = &P.st->stopped;
     for (int64_t k = 0; k < m; ++k) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, nullptr, u32, st, ds->sm_count, s));  // u = A q
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, u32, w, nullptr, st, ds->sm_count, s));    // w = A^T u
-        lz_update_kernel<<<1, 1024, 0, s>>>(n, m, static_cast<int>(k), tol, st, alpha, beta, q, w, vold, V, q32);
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, ds->sm_count, s));  // u = A q
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s));    // w = A^T u
+        lz_update_kernel<<<1, 1024, 0, s>>>(n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q, P.w, P.vold,
+                                            P.V, P.q32);
         count_launch();
         PSDGB_CUDA_TRY(cudaGetLastError());
     }
-
-    LzState hst{};
-    std::vector<double> ha(m + 1), hb(m + 1);
-    PSDGB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
-    PSDGB_CUDA_TRY(cudaMemcpyAsync(ha.data(), alpha, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
-    PSDGB_CUDA_TRY(cudaMemcpyAsync(hb.data(), beta, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
-    PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
-    if (h_alpha) for (int64_t i = 0; i < m; ++i) h_alpha[i] = ha[i];
-    if (h_beta) for (int64_t i = 0; i < m; ++i) h_beta[i] = hb[i];
-
-    const int64_t nb = hst.nb_iter;
-    res->nb_iter = nb;
-    if (nb == 0) {
-        res->lo = 0.0;
-        res->up = 1.0;
-        return PSDGB_OK;
-    }
-    double theta = 0.0;
-    std::vector<double> u(nb);
-    tridiag_largest_eigenpair(ha.data(), hb.data(), nb, &theta, u.data());
-    PSDGB_CUDA_TRY(cudaMemcpyAsync(uk, u.data(), sizeof(double) * nb, cudaMemcpyHostToDevice, s));
+    lz_tridiag_kernel<<<1, 32, 0, s>>>(P.st, P.alpha, P.beta, P.uk, P.work);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
     {
         int64_t blocks = (n + 255) / 256;
         if (blocks > 4096) blocks = 4096;
-        lz_ritz_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(n, nb, V, uk, y, q32);
+        lz_ritz_kernel<<<static_cast<unsigned>(blocks), 256, 0, s>>>(n, P.st, P.V, P.uk, P.y, P.q32, d_ritz_out);
         count_launch();
         PSDGB_CUDA_TRY(cudaGetLastError());
     }
+    const int* no_ritz = &P.st->no_ritz;
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, nullptr, u32, nullptr, ds->sm_count, s));  // A y
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, u32, ry, nullptr, nullptr, ds->sm_count, s));   // A^T A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, no_ritz, ds->sm_count, s));  // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.ry, nullptr, no_ritz, ds->sm_count, s));   // A^T A y
     } else {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, q32, ry, nullptr, nullptr, ds->sm_count, s));   // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, P.ry, nullptr, no_ritz, ds->sm_count, s));   // A y
     }
-    lz_resid_kernel<<<1, 1024, 0, s>>>(n, theta, ry, y, st);
+    lz_resid_kernel<<<1, 1024, 0, s>>>(n, P.ry, P.y, P.st);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
-    PSDGB_CUDA_TRY(cudaMemcpyAsync(&hst, st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+    return PSDGB_OK;
+}
+
+psdgb_status lanczos_read(void* d_state, int64_t n, int64_t max_iter, cudaStream_t s, LanczosResult* res,
+                          double* h_alpha, double* h_beta) {
+    const int64_t m0 = max_iter < n ? max_iter : n;
+    const int64_t m = m0 < 0 ? 0 : m0;
+    const LzPtrs P = lz_ptrs(d_state, n, m);
+    LzState hst{};
+    std::vector<double> ha(m + 1, 0.0), hb(m + 1, 0.0);
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(&hst, P.st, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+    if (m > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(ha.data(), P.alpha, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(hb.data(), P.beta, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+    }
     PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
-    const double rnorm = std::sqrt(hst.resid_norm2);
-    res->theta = theta;
-    res->lo = std::sqrt(theta);
-    res->up = std::sqrt(theta + rnorm);
+    if (h_alpha) for (int64_t i = 0; i < max_iter; ++i) h_alpha[i] = (i < m) ? ha[i] : 0.0;
+    if (h_beta) for (int64_t i = 0; i < max_iter; ++i) h_beta[i] = (i < m) ? hb[i] : 0.0;
+    res->nb_iter = hst.nb_iter;
+    res->theta = hst.theta;
+    res->lo = hst.lo;
+    res->up = hst.up;
     return PSDGB_OK;
 }
 

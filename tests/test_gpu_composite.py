@@ -175,3 +175,77 @@ def test_reference_method_mapping(psd):
         t = to_dev(x * 7.0)
         fn(t)
         assert rp.rel_frobenius(from_dev(t), proj * 7.0) <= tol
+
+
+def _async_buffers(psd, n, precision, max_iter=20):
+    import torch
+
+    lib = psd._capi.lib()
+    ws = torch.empty(psd.workspace_size(n, precision), dtype=torch.uint8, device="cuda")
+    lz = torch.empty(lib.psdgb_lanczos_state_size(n, max_iter), dtype=torch.uint8, device="cuda")
+    return ws, lz
+
+
+def _run_async(psd, t, precision, ws, lz, warm=None, ritz=None, stream=None, max_iter=20):
+    import ctypes
+
+    import torch
+
+    lib = psd._capi.lib()
+    n = t.shape[0]
+    s = stream if stream is not None else torch.cuda.current_stream()
+    st = lib.psdgb_composite_auto_scale_async(
+        precision, psd.SCHEDULE_FP32, ctypes.c_void_p(t.data_ptr()), n, max_iter, 1e-10, psd.DEFAULT_SEED, 0,
+        ctypes.c_void_p(warm.data_ptr()) if warm is not None else None,
+        ctypes.c_void_p(ritz.data_ptr()) if ritz is not None else None,
+        ctypes.c_void_p(ws.data_ptr()), ws.numel(), ctypes.c_void_p(lz.data_ptr()), lz.numel(),
+        ctypes.c_void_p(s.cuda_stream))
+    psd._capi.check(st, "psdgb_composite_auto_scale_async")
+
+
+def test_async_matches_sync_and_warm_start(psd):
+    import torch
+
+    prec = psd.PRECISIONS["fp16x3"]
+    x = gaussian_sym(260, seed=21)
+    want, _ = run(psd, x, "fp16x3", auto_scale=True)
+    ws, lz = _async_buffers(psd, 260, prec)
+    t = to_dev(x)
+    ritz = torch.empty(260, dtype=torch.float64, device="cuda")
+    _run_async(psd, t, prec, ws, lz, ritz=ritz)
+    torch.cuda.synchronize()
+    assert psd._capi.lib().psdgb_check_device_error() == 0
+    assert np.array_equal(from_dev(t), want)
+    # ADMM-style repeat call: a slightly changed matrix, warm-started from the previous Ritz vector.
+    e = np.random.default_rng(22).standard_normal((260, 260))
+    x2 = x + 1e-2 * 0.5 * (e + e.T)
+    t2 = to_dev(x2)
+    _run_async(psd, t2, prec, ws, lz, warm=ritz, max_iter=20)
+    torch.cuda.synchronize()
+    proj2, _ = rp.eig_psd(x2)
+    assert rp.rel_frobenius(from_dev(t2), proj2) <= 1e-4
+
+
+def test_async_path_captures_in_a_cuda_graph(psd):
+    import torch
+
+    prec = psd.PRECISIONS["fp16x3"]
+    n = 300
+    x = gaussian_sym(n, seed=23)
+    want, _ = run(psd, x, "fp16x3", auto_scale=True)
+    ws, lz = _async_buffers(psd, n, prec)
+    static_in = to_dev(np.zeros((n, n)))
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):  # warm-up outside capture
+        _run_async(psd, static_in, prec, ws, lz, stream=side)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        _run_async(psd, static_in, prec, ws, lz)
+    for _ in range(2):
+        static_in.copy_(to_dev(x))
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(from_dev(static_in), want)
