@@ -55,6 +55,9 @@ def parse_args():
     ap.add_argument("--no-side-by-side", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=4096)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving session")
+    ap.add_argument("--no-batch", action="store_true", help="skip the block-diagonal batch session")
+    ap.add_argument("--only-batch", action="store_true", help="run only the block-diagonal batch session")
+    ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--workload", choices=["spectrum", "gaussian"], default="spectrum",
                     help="spectrum: Q diag(lambda) Q^T (the n=8192 configuration); gaussian: (G+G^T)/2 scaled to "
@@ -297,6 +300,93 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
 
 
 # ---------------------------------------------------------------------------
+# block-diagonal batch: 4096 uneven blocks
+# ---------------------------------------------------------------------------
+
+def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_sample: int = 8) -> dict:
+    """4096 blocks, n log-uniform in [16, 512] (seeded), entries (G + G^T)/2,
+    stored FP32; the whole batch projected by one plan inside one captured CUDA
+    graph, against the same blocks projected one call at a time."""
+    import numpy as np
+    import torch
+
+    import psd_projection_gb300 as psd
+    from oracle import reference_port as rp
+    from psd_projection_gb300.batch import BatchPlan
+
+    rng = np.random.default_rng(seed)
+    sizes = [int(round(v)) for v in np.exp(rng.uniform(np.log(16), np.log(512), count))]
+    offs = np.concatenate([[0], np.cumsum([n * n for n in sizes])])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    pristine = torch.empty(int(offs[-1]), dtype=torch.float64, device="cuda")
+    for b, n in enumerate(sizes):
+        G = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+        pristine[offs[b]:offs[b + 1]].copy_((0.5 * (G + G.T)).float().double().reshape(-1))
+    torch.cuda.synchronize()
+    plan = BatchPlan(sizes)
+    scratch = pristine.clone()
+    best = plan.autotune(scratch)
+    info = plan.info()
+    work = pristine.clone()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        plan.project(scratch, stream=side)
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        work.copy_(pristine)
+        plan.project(work)
+    graph.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(replays):
+        graph.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1) / replays
+    # copy-only cost inside the graph, for reference
+    e0.record()
+    for _ in range(replays):
+        scratch.copy_(pristine)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_copy = e0.elapsed_time(e1) / replays
+    # one call at a time (the reference's usage: one projection per block)
+    one = pristine.clone()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for b, n in enumerate(sizes):
+        psd.composite(one[offs[b]:offs[b + 1]].view(n, n))
+    torch.cuda.synchronize()
+    ms_one = (time.perf_counter() - t0) * 1e3
+    diffs = []
+    for b, n in enumerate(sizes):
+        a = work[offs[b]:offs[b + 1]]
+        c = one[offs[b]:offs[b + 1]]
+        diffs.append(float(torch.linalg.vector_norm(a - c) / torch.linalg.vector_norm(c)))
+    evd = {}
+    for b in sorted(range(count), key=lambda i: -sizes[i])[:evd_sample // 2] + list(range(evd_sample // 2)):
+        n = sizes[b]
+        x = pristine[offs[b]:offs[b + 1]].cpu().numpy().reshape(n, n).T
+        proj, _ = rp.eig_psd(x)
+        y = work[offs[b]:offs[b + 1]].cpu().numpy().reshape(n, n).T
+        evd[str(n)] = rp.rel_frobenius(y, proj)
+    plan.close()
+    dense = sum(62.0 * n ** 3 for n in sizes)
+    return {"blocks": count, "sizes": "log-uniform [16, 512], seed 0", "sum_n3": float(sum(n ** 3 for n in sizes)),
+            "ms_per_batch_graph": ms_batch, "ms_input_copy_in_graph": ms_copy, "ms_one_call_at_a_time": ms_one,
+            "speedup_vs_one_call_at_a_time": ms_one / ms_batch, "batches_per_s": 1e3 / ms_batch,
+            "dense_equiv_tflops": dense / (ms_batch / 1e3) / 1e12,
+            "max_rel_diff_vs_one_call": max(diffs), "rel_frobenius_err_vs_evd_sample": evd,
+            "autotune": {"best_ms": best, "acc_mode": info["acc_mode"], "tile_order": info["tile_order"],
+                         "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"]}}
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline: FP64 LAPACK dsyevd projection (eig_FP64_psd's math)
 # ---------------------------------------------------------------------------
 
@@ -443,6 +533,9 @@ def run_ours(args, rank, world):
                                      "fp32_simt": "plain FP32 (CUDA cores)"}.get(name, name)}
         out["side_by_side"] = side
 
+    if not args.no_batch:
+        out["batched"] = batched_session(count=args.batch_count)
+
     if not args.no_serve:
         sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
         out["serving"] = {
@@ -518,6 +611,9 @@ def run_reference(args, rank, world):
 def main():
     args = parse_args()
     rank, world = dist_setup()
+    if args.only_batch:
+        print(json.dumps({"batched": batched_session(count=args.batch_count)}))
+        return
     res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
     if rank == 0 and res is not None:
         print(json.dumps(res))

@@ -231,11 +231,34 @@ psdgb_status psdgb_server_poll(psdgb_server* server, int wait, psdgb_completion*
 psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queued, size_t* bytes_used,
                                 uint64_t* completed);
 
+/* ---- block-diagonal batches ---------------------------------------------------
+ * No counterpart in the reference, which projects one matrix per call.  A plan
+ * for `count` symmetric blocks of the given sizes (0..4096) projects all of
+ * them with ~35 kernel launches (independent of count): one CTA per block for
+ * the Lanczos bound, one persistent tensor-core kernel per product over the
+ * tiles of every block.  The blocks are packed column-major, one after the
+ * other (block b starts at element sum_{c<b} n_c^2), and projected in place —
+ * the layout of a block-diagonal SDP iterate.  psdgb_batch_project is
+ * asynchronous and allocates nothing (the plan owns its device memory), so
+ * it can be captured in a CUDA graph.  psdgb_batch_autotune times every
+ * accumulator configuration and tile order on the caller's scratch blocks
+ * (overwritten) and keeps the fastest. */
+typedef struct psdgb_batch psdgb_batch;
+psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
+                                psdgb_batch** out);
+psdgb_status psdgb_batch_destroy(psdgb_batch* batch);
+psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements, size_t* device_bytes,
+                              int64_t* num_tiles, int* acc_mode, int* tile_order);
+psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
+psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Accumulator configuration of the tensor-core products of single-matrix
- * calls: 0 = four interleaved K accumulators (default), 1 = two accumulators
- * double-buffered (the epilogue of one tile overlaps the next tile's MMAs),
- * 2 = one accumulator, four buffers.  Returns the previous value. */
+ * calls: -1 = automatic (default: four interleaved K accumulators for long
+ * FP32-class products, double-buffered ones otherwise), 0 = four interleaved
+ * K accumulators, 1 = two accumulators double-buffered (the epilogue of one
+ * tile overlaps the next tile's MMAs), 2 = one accumulator, four buffers.
+ * Returns the previous value. */
 int psdgb_set_product_config(int acc_mode);
 
 /* Product-kernel timing: when enabled, the library records a CUDA event pair

@@ -27,7 +27,7 @@ CFLAGS = [
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
 ]
 SOURCES = ["capi.cu", "composite.cu", "elem.cu", "lanczos.cu", "gemm_simt.cu", "gemm_tc.cu", "refapi.cu",
-           "static_scratch.cu", "serve.cu"]
+           "static_scratch.cu", "serve.cu", "batch.cu"]
 
 
 def nvcc() -> str:

@@ -1,0 +1,637 @@
+// batch.cu — projection of a block-diagonal iterate: many independent
+// symmetric blocks of uneven sizes in one pass.
+//
+// A block-diagonal SDP iterate is projected block by block; the reference
+// offers only one call per block (each a full chain of ~100 library calls).
+// Here the whole batch is one plan and ~35 kernel launches, independent of
+// the number of blocks, so it can be captured in one CUDA graph:
+//
+//   batch_to_f32      every block's upper triangle -> FP32 symmetric copy
+//   lz_batch_kernel   one CTA per block runs the whole Lanczos bound of its
+//                     block (recurrence, tridiagonal eigenpair, Ritz residual)
+//                     and leaves the block's scale 1/up on the device
+//   batch_split       scaled operand terms into one strided layout
+//   3 x steps         grouped persistent tensor-core products over the tile
+//                     list of all blocks (gemm_tc.cu)
+//   batch_split (X)   Xs = X / up per block
+//   1 dual product    (X + up (Xs A + A Xs)/2) / 2 into the caller's blocks
+//
+// Layout: blocks are padded to np = n rounded up to 128 and shelf-packed into
+// a strip of width ld = max np (blocks of one size side by side, a shelf per
+// row band), so a single TMA descriptor per operand plane covers every block.
+// The autotuner times the first product under each accumulator configuration
+// and tile order (LPT: largest K first, or block order) and keeps the fastest.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "internal.h"
+#include "tridiag.cuh"
+
+
+namespace {
+
+using namespace psdgb;
+
+constexpr int LZ_THREADS = 512;   // Lanczos: one CTA per block
+constexpr int COPY_THREADS = 256;  // 32 x 8 transpose tiles
+constexpr int COPY_SPLIT = 16;     // CTAs per block for the copy / split kernels
+
+struct BatchState {
+    double theta, lo, up, scale, inv_scale;
+    int nb_iter, pad;
+};
+
+struct LzBlockDesc {
+    int n;
+    int ld4;
+    int m;
+    int pad;
+    long long a32_off;  // floats
+    long long vec_off;  // doubles: V (n*m) | alpha, beta, uk (m+1 each) | work (4(m+1))
+    long long x_off;    // doubles into the packed FP64 blocks
+};
+
+inline int64_t up_to(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+// Block-wide FP64 sum through shared memory: every thread stores its
+// partial, warp 0 adds blockDim/32 values per lane and reduces across lanes,
+// and the result is broadcast.  About 21 FP64 warp instructions per sum
+// instead of 10 per warp for shuffle trees in every warp (FP64 issue is
+// scarce on this part).  part holds blockDim.x doubles, red one.
+__device__ double cta_sum(double v, double* part, double* red) {
+    __syncthreads();
+    part[threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < static_cast<int>(blockDim.x); i += 32) t += part[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+// y[c] = sum_r A[c*ld4 + r] x[r] for the block's symmetric FP32 matrix.
+// Each warp takes four columns at a time and each lane keeps up to sixteen
+// float4 loads in flight (the columns are L2-resident and the loop is
+// latency-bound otherwise).  Lane partial sums and the shuffle reduction are
+// FP32 (a column here is at most 4096 long), one FP64 conversion per column:
+// on this part a warp-wide FP64 add occupies the FP64 pipe for many cycles,
+// and FP64 shuffle reductions made the whole bound FP64-bound.
+__device__ void cta_matvec(const float* __restrict__ A, int n, int ld4, const float* xs, double* y64, float* y32) {
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32, nw = blockDim.x / 32;
+    const float4* xs4 = reinterpret_cast<const float4*>(xs);
+    const int kv = ld4 / 4;
+    for (int c0 = warp * 4; c0 < n; c0 += nw * 4) {
+        float s[4] = {0.f, 0.f, 0.f, 0.f};
+        const float4* col[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) col[j] = reinterpret_cast<const float4*>(A + static_cast<int64_t>(min(c0 + j, n - 1)) * ld4);
+#pragma unroll 4
+        for (int k = lane; k < kv; k += 32) {
+            const float4 b = xs4[k];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float4 a = __ldg(col[j] + k);
+                s[j] = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, s[j]))));
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            float acc = s[j];
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            const int c = c0 + j;
+            if (lane == 0 && c < n) {
+                if (y64) y64[c] = static_cast<double>(acc);
+                if (y32) y32[c] = acc;
+            }
+        }
+    }
+}
+
+// The Lanczos bound of one block per CTA (src/lanczos.cu:41-293, as in lanczos.cu).
+__global__ void __launch_bounds__(LZ_THREADS, 2) lz_batch_kernel(const LzBlockDesc* __restrict__ descs,
+                                                              const float* __restrict__ a32, double* vec,
+                                                              BatchState* states, double tol, uint64_t seed,
+                                                              int residual_mode) {
+    extern __shared__ double sh[];
+    __shared__ double red[32];
+    __shared__ double part[LZ_THREADS];
+    const LzBlockDesc d = descs[blockIdx.x];
+    const int n = d.n, ld4 = d.ld4, m = d.m;
+    BatchState* st = states + blockIdx.x;
+    if (m <= 0) {
+        if (threadIdx.x == 0) *st = BatchState{0.0, 0.0, 1.0, 1.0, 1.0, 0, 0};
+        return;
+    }
+    double* q = sh;
+    double* w = q + ld4;
+    double* vold = w + ld4;
+    double* y = vold + ld4;
+    double* ry = y + ld4;
+    float* x32 = reinterpret_cast<float*>(ry + ld4);  // ld4 floats
+    float* u32 = x32 + ld4;
+    const float* A = a32 + d.a32_off;
+    double* V = vec + d.vec_off;
+    double* alpha = V + static_cast<int64_t>(n) * m;
+    double* beta = alpha + (m + 1);
+    double* uk = beta + (m + 1);
+    double* work = uk + (m + 1);
+    for (int i = threadIdx.x; i < ld4; i += blockDim.x) {
+        x32[i] = 0.f;
+        u32[i] = 0.f;
+    }
+    // start vector (uniform (0, 1] from the seed), normalised
+    double ss = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint64_t h = splitmix64(seed ^ splitmix64(static_cast<uint64_t>(i)));
+        const double u = static_cast<double>((h >> 11) + 1) * 0x1.0p-53;
+        q[i] = u;
+        ss += u * u;
+    }
+    const double nrm = sqrt(cta_sum(ss, part, red));
+    const double inv0 = nrm != 0.0 ? 1.0 / nrm : 1.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        q[i] *= inv0;
+        V[i] = q[i];
+        vold[i] = 0.0;
+        x32[i] = static_cast<float>(q[i]);
+    }
+    double beta_old = 0.0;
+    int nb = 0;
+    for (int k = 0; k < m; ++k) {
+        __syncthreads();
+        cta_matvec(A, n, ld4, x32, nullptr, u32);  // u = A q
+        __syncthreads();
+        cta_matvec(A, n, ld4, u32, w, nullptr);    // w = A^T u
+        __syncthreads();
+        double s = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) s += q[i] * w[i];
+        const double a = cta_sum(s, part, red);
+        s = 0.0;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double v = w[i] - a * q[i] - beta_old * vold[i];
+            w[i] = v;
+            s += v * v;
+        }
+        const double b = sqrt(cta_sum(s, part, red));
+        if (threadIdx.x == 0) {
+            alpha[k] = a;
+            beta[k] = b;
+        }
+        if ((b <= tol * a && k > 1) || b == 0.0) break;
+        const double binv = 1.0 / b;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            const double qn = w[i] * binv;
+            vold[i] = q[i];
+            q[i] = qn;
+            x32[i] = static_cast<float>(qn);
+            if (k < m - 1) V[static_cast<int64_t>(k + 1) * n + i] = qn;
+        }
+        beta_old = b;
+        nb = k + 1;
+    }
+    __syncthreads();
+    if (nb == 0) {
+        if (threadIdx.x == 0) *st = BatchState{0.0, 0.0, 1.0, 1.0, 1.0, 0, 0};
+        return;
+    }
+    double theta;
+    if (nb == 1) {
+        theta = alpha[0];
+        if (threadIdx.x == 0) uk[0] = 1.0;
+    } else {
+        if (threadIdx.x < 32) {
+            const double t = warp_tridiag_top(alpha, beta, nb, uk, work);
+            if (threadIdx.x == 0) red[0] = t;
+        }
+        __syncthreads();
+        theta = red[0];
+    }
+    __syncthreads();
+    // Ritz vector y = V u and the residual
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < nb; ++j) s += V[static_cast<int64_t>(j) * n + i] * uk[j];
+        y[i] = s;
+        x32[i] = static_cast<float>(s);
+    }
+    __syncthreads();
+    if (residual_mode == PSDGB_RESIDUAL_EXACT) {
+        cta_matvec(A, n, ld4, x32, nullptr, u32);
+        __syncthreads();
+        cta_matvec(A, n, ld4, u32, ry, nullptr);
+    } else {
+        cta_matvec(A, n, ld4, x32, ry, nullptr);
+    }
+    __syncthreads();
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double r = ry[i] - theta * y[i];
+        s += r * r;
+    }
+    const double rn = sqrt(cta_sum(s, part, red));
+    if (threadIdx.x == 0) {
+        const double up = sqrt(theta + rn);
+        const double scale = up > 0.0 ? up : 1.0;
+        *st = BatchState{theta, sqrt(theta), up, scale, 1.0 / scale, nb, 0};
+    }
+}
+
+// The symmetric matrix defined by the upper triangle of column-major X_b,
+// written as FP32 rows (a32, n x ld4) — one CTA per block, 32x32 transposes.
+__global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const double* __restrict__ x,
+                                    float* a32) {
+    __shared__ double sm[32][33];
+    const LzBlockDesc d = descs[blockIdx.x];
+    if (d.n == 0) return;
+    const int n = d.n, ld4 = d.ld4;
+    const double* X = x + d.x_off;
+    float* A = a32 + d.a32_off;
+    const int tx = threadIdx.x % 32, ty0 = threadIdx.x / 32;
+    const int nt_r = (n + 31) / 32, nt_c = (ld4 + 31) / 32;
+    for (int t = blockIdx.y; t < nt_r * nt_c; t += gridDim.y) {
+        const int bi = t / nt_c, bj = t % nt_c;
+        const int rbase = (bi <= bj) ? bi * 32 : bj * 32;
+        const int cbase = (bi <= bj) ? bj * 32 : bi * 32;
+        __syncthreads();
+        for (int ty = ty0; ty < 32; ty += 8) {
+            const int r = rbase + tx, c = cbase + ty;
+            sm[ty][tx] = (r < n && c < n) ? X[r + static_cast<int64_t>(c) * n] : 0.0;
+        }
+        __syncthreads();
+        for (int ty = ty0; ty < 32; ty += 8) {
+            const int i = bi * 32 + ty, j = bj * 32 + tx;
+            if (i >= n || j >= ld4) continue;
+            double v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
+            if (j >= n) v = 0.0;
+            A[static_cast<int64_t>(i) * ld4 + j] = static_cast<float>(v);
+        }
+    }
+}
+
+// Operand terms of block b into the strided layout: from the FP32 copy
+// (from_x == 0) or the FP64 input (from_x != 0, upper triangle), times the
+// block's 1/up; zero in the padding of the block's np x np region.
+__global__ void batch_split_kernel(const LzBlockDesc* __restrict__ lz, const BlockDesc* __restrict__ blocks,
+                                   const BatchState* __restrict__ states, const float* __restrict__ a32,
+                                   const double* __restrict__ x, int from_x, SplitMat out, int fmt, int64_t ld) {
+    __shared__ double sm[32][33];
+    const LzBlockDesc d = lz[blockIdx.x];
+    const BlockDesc bd = blocks[blockIdx.x];
+    const double inv = states[blockIdx.x].inv_scale;
+    const int n = d.n, np = bd.np;
+    const int tx = threadIdx.x % 32, ty0 = threadIdx.x / 32;
+    const int nt = np / 32;
+    const double* X = x + d.x_off;
+    const float* A = a32 + d.a32_off;
+    for (int t = blockIdx.y; t < nt * nt; t += gridDim.y) {
+        const int bi = t / nt, bj = t % nt;
+        if (from_x) {
+            const int rbase = (bi <= bj) ? bi * 32 : bj * 32;
+            const int cbase = (bi <= bj) ? bj * 32 : bi * 32;
+            __syncthreads();
+            for (int ty = ty0; ty < 32; ty += 8) {
+                const int r = rbase + tx, c = cbase + ty;
+                sm[ty][tx] = (r < n && c < n) ? X[r + static_cast<int64_t>(c) * n] : 0.0;
+            }
+            __syncthreads();
+        }
+        for (int ty = ty0; ty < 32; ty += 8) {
+            const int i = bi * 32 + ty, j = bj * 32 + tx;
+            double v = 0.0;
+            if (i < n && j < n) {
+                if (from_x)
+                    v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
+                else
+                    v = A[static_cast<int64_t>(i) * d.ld4 + j];
+            }
+            split_store(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j,
+                        static_cast<float>(v * inv));
+        }
+    }
+}
+
+}  // namespace
+
+struct psdgb_batch {
+    int precision = 0, schedule = 0, fmt = 0;
+    int64_t count = 0, ld = 0, rows = 0, max_iter = 20;
+    double tol = 1e-10;
+    uint64_t seed = 0x5eed5eedull;
+    std::vector<int64_t> n;
+    int64_t total_elems = 0;  // sum n^2 (the packed FP64 input)
+    // device
+    void* dev = nullptr;
+    size_t dev_bytes = 0;
+    BlockDesc* blocks = nullptr;
+    LzBlockDesc* lz = nullptr;
+    TileDesc* tiles[2] = {nullptr, nullptr};  // 0: LPT order, 1: block order
+    BatchState* states = nullptr;
+    float* a32 = nullptr;
+    double* vec = nullptr;
+    SplitMat A{}, A2{}, A3{};
+    int64_t num_tiles = 0;
+    size_t lz_smem = 0;
+    // tuning
+    int acc_mode = ACC_1X4;
+    int order = 0;
+};
+
+namespace {
+
+psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    const int count = static_cast<int>(b->count);
+    const dim3 copy_grid(count, COPY_SPLIT);
+    batch_to_f32_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, d_blocks, b->a32);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    lz_batch_kernel<<<count, LZ_THREADS, b->lz_smem, s>>>(b->lz, b->a32, b->vec, b->states, b->tol, b->seed,
+                                                        PSDGB_RESIDUAL_REFERENCE);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    batch_split_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 0, b->A,
+                                                         b->fmt, b->ld);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    PrecisionInfo pi{};
+    precision_info(b->precision, &pi);
+    const bool dual_step = pi.nprod == 1;
+    GroupWork gw{b->tiles[b->order], b->blocks};
+    float coeffs[64];
+    const int steps = psdgb_filter_coefficients(b->schedule, coeffs, 21);
+    auto base = [&]() {
+        EpiParams e{};
+        e.fmt = b->fmt;
+        e.ld = static_cast<int>(b->ld);
+        e.acc_scale = 1.0f;
+        e.up = 1.0;
+        return e;
+    };
+    for (int k = 0; k < steps; ++k) {
+        EpiParams e1 = base();
+        e1.kind = EPI_STORE;
+        e1.out = b->A2;
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A, b->A, b->ld, b->rows, e1, gw, b->num_tiles, 0,
+                                s));
+        EpiParams e2 = base();
+        e2.kind = EPI_STORE;
+        e2.out = b->A3;
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, e2, gw, b->num_tiles,
+                                0, s));
+        EpiParams e3 = base();
+        e3.kind = EPI_STEP;
+        e3.a = coeffs[3 * k];
+        e3.b = coeffs[3 * k + 1];
+        e3.c = coeffs[3 * k + 2];
+        e3.A = b->A;
+        e3.A3 = b->A3;
+        e3.out = b->A;
+        if (dual_step) {
+            e3.dual = 1;
+            e3.acc_scale = 0.5f;
+        }
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A3, b->A2, b->ld, b->rows, e3, gw, b->num_tiles,
+                                0, s));
+    }
+    batch_split_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 1, b->A2,
+                                                         b->fmt, b->ld);
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
+    EpiParams ef = base();
+    ef.kind = EPI_FINAL;
+    ef.dual = 1;
+    ef.acc_scale = 0.5f;
+    ef.x64 = d_blocks;
+    ef.out64 = d_blocks;
+    return gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, b->num_tiles, 0, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
+                                psdgb_batch** out) {
+    if (!out || (count > 0 && !sizes) || count < 0 || count > (1 << 24)) {
+        set_error("psdgb_batch_create: bad arguments");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi) || precision == PSDGB_PREC_FP32_SIMT) {
+        set_error("psdgb_batch_create: the batch runs the tensor-core precisions");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
+        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    auto b = new psdgb_batch();
+    b->precision = precision;
+    b->schedule = schedule;
+    b->fmt = pi.fmt;
+    b->count = count;
+    b->n.assign(sizes, sizes + count);
+    int64_t maxnp = 128;
+    for (int64_t i = 0; i < count; ++i) {
+        if (sizes[i] < 0 || sizes[i] > 4096) {
+            delete b;
+            set_error("psdgb_batch_create: block sizes must lie in [0, 4096]");
+            return PSDGB_ERR_INVALID_ARGUMENT;
+        }
+        maxnp = std::max<int64_t>(maxnp, up_to(std::max<int64_t>(sizes[i], 1), 128));
+    }
+    b->ld = maxnp;
+    // Shelf packing: blocks sorted by np (largest first); a shelf of height np
+    // holds ld / np blocks side by side.
+    std::vector<int64_t> order(count);
+    std::iota(order.begin(), order.end(), 0);
+    auto npof = [&](int64_t i) { return up_to(std::max<int64_t>(b->n[i], 1), 128); };
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return npof(a) > npof(c); });
+    std::vector<BlockDesc> bd(count);
+    std::vector<LzBlockDesc> lz(count);
+    int64_t row = 0, col = 0, shelf_h = 0;
+    for (int64_t idx : order) {
+        const int64_t np = npof(idx);
+        if (shelf_h != np || col + np > b->ld) {  // new shelf
+            row += shelf_h;
+            shelf_h = np;
+            col = 0;
+        }
+        bd[idx].row_base = static_cast<int>(row);
+        bd[idx].col_base = static_cast<int>(col);
+        bd[idx].np = static_cast<int>(np);
+        bd[idx].n = static_cast<int>(b->n[idx]);
+        col += np;
+    }
+    b->rows = row + shelf_h;
+    int64_t xoff = 0, aoff = 0, voff = 0;
+    size_t max_smem = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        const int64_t n = b->n[i], ld4 = up_to(std::max<int64_t>(n, 1), 4);
+        const int64_t m = std::min<int64_t>(b->max_iter, n);
+        bd[i].x_off = xoff;
+        lz[i] = LzBlockDesc{static_cast<int>(n), static_cast<int>(ld4), static_cast<int>(m), 0, aoff, voff, xoff};
+        xoff += n * n;
+        aoff += up_to(n * ld4, 64);
+        voff += up_to(n * m + 7 * (m + 1), 32);
+        max_smem = std::max<size_t>(max_smem, 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float));
+    }
+    b->total_elems = xoff;
+    b->lz_smem = max_smem;
+    // Tile lists: LPT (largest K first) and block order.
+    std::vector<TileDesc> tl_block;
+    for (int64_t i = 0; i < count; ++i) {
+        const int nt = bd[i].np / 128;
+        for (int bi = 0; bi < nt; ++bi)
+            for (int bj = 0; bj <= bi; ++bj) tl_block.push_back(TileDesc{static_cast<int>(i), bi, bj, 0});
+    }
+    std::vector<TileDesc> tl_lpt = tl_block;
+    std::stable_sort(tl_lpt.begin(), tl_lpt.end(),
+                     [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });
+    b->num_tiles = static_cast<int64_t>(tl_block.size());
+    // Device memory: tables | states | FP32 copies | Lanczos vectors | operand planes.
+    const size_t plane = static_cast<size_t>(b->rows) * b->ld * 2;
+    const int nterms = format_terms(b->fmt);
+    auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t sz_blocks = a256(sizeof(BlockDesc) * std::max<int64_t>(count, 1));
+    const size_t sz_lz = a256(sizeof(LzBlockDesc) * std::max<int64_t>(count, 1));
+    const size_t sz_tiles = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles, 1));
+    const size_t sz_states = a256(sizeof(BatchState) * std::max<int64_t>(count, 1));
+    const size_t sz_a32 = a256(sizeof(float) * std::max<int64_t>(aoff, 1));
+    const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
+    const size_t sz_ops = 3 * nterms * a256(plane);
+    b->dev_bytes = sz_blocks + sz_lz + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_ops;
+    cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        set_error("psdgb_batch_create: device allocation failed");
+        return PSDGB_ERR_OUT_OF_MEMORY;
+    }
+    char* p = static_cast<char*>(b->dev);
+    b->blocks = reinterpret_cast<BlockDesc*>(p);
+    p += sz_blocks;
+    b->lz = reinterpret_cast<LzBlockDesc*>(p);
+    p += sz_lz;
+    b->tiles[0] = reinterpret_cast<TileDesc*>(p);
+    p += sz_tiles;
+    b->tiles[1] = reinterpret_cast<TileDesc*>(p);
+    p += sz_tiles;
+    b->states = reinterpret_cast<BatchState*>(p);
+    p += sz_states;
+    b->a32 = reinterpret_cast<float*>(p);
+    p += sz_a32;
+    b->vec = reinterpret_cast<double*>(p);
+    p += sz_vec;
+    SplitMat* mats[3] = {&b->A, &b->A2, &b->A3};
+    for (int mi = 0; mi < 3; ++mi)
+        for (int t = 0; t < 3; ++t) {
+            mats[mi]->term[t] = (t < nterms) ? p : nullptr;
+            if (t < nterms) p += a256(plane);
+        }
+    for (int64_t i = 0; i < count; ++i) bd[i].up_dev = &b->states[i].scale;
+    if (count > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpy(b->blocks, bd.data(), sizeof(BlockDesc) * count, cudaMemcpyHostToDevice));
+        PSDGB_CUDA_TRY(cudaMemcpy(b->lz, lz.data(), sizeof(LzBlockDesc) * count, cudaMemcpyHostToDevice));
+    }
+    if (b->num_tiles > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[0], tl_lpt.data(), sizeof(TileDesc) * b->num_tiles,
+                                  cudaMemcpyHostToDevice));
+        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[1], tl_block.data(), sizeof(TileDesc) * b->num_tiles,
+                                  cudaMemcpyHostToDevice));
+    }
+    // Padding rows/columns between blocks are never read; zero the planes once
+    // so every TMA box reads finite values.
+    PSDGB_CUDA_TRY(cudaMemset(b->A.term[0], 0, sz_ops));
+    if (b->lz_smem > 48 * 1024)
+        PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            static_cast<int>(b->lz_smem)));
+    *out = b;
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_batch_destroy(psdgb_batch* b) {
+    if (!b) return PSDGB_OK;
+    cudaDeviceSynchronize();
+    if (b->dev) cudaFree(b->dev);
+    delete b;
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_batch_info(const psdgb_batch* b, int64_t* total_elements, size_t* device_bytes,
+                              int64_t* num_tiles, int* acc_mode, int* tile_order) {
+    if (!b) return PSDGB_ERR_INVALID_ARGUMENT;
+    if (total_elements) *total_elements = b->total_elems;
+    if (device_bytes) *device_bytes = b->dev_bytes;
+    if (num_tiles) *num_tiles = b->num_tiles;
+    if (acc_mode) *acc_mode = b->acc_mode;
+    if (tile_order) *tile_order = b->order;
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream) {
+    if (!b || (b->total_elems > 0 && !d_blocks)) {
+        set_error("psdgb_batch_project: bad arguments");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (b->count == 0) return PSDGB_OK;
+    return batch_enqueue(b, d_blocks, static_cast<cudaStream_t>(stream));
+}
+
+psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void* stream, double* best_ms) {
+    if (!b || (b->total_elems > 0 && !d_scratch_blocks)) {
+        set_error("psdgb_batch_autotune: bad arguments");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (b->count == 0) return PSDGB_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    PSDGB_CUDA_TRY(cudaEventCreate(&e0));
+    PSDGB_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_acc = b->acc_mode, best_order = b->order;
+    const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
+    for (int ai = 0; ai < 3; ++ai) {
+        for (int o = 0; o < 2; ++o) {
+            b->acc_mode = accs[ai];
+            b->order = o;
+            PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
+            PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
+            PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
+            PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
+            PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_acc = accs[ai];
+                best_order = o;
+            }
+        }
+    }
+    b->acc_mode = best_acc;
+    b->order = best_order;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_ms) *best_ms = best;
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    return finish(ds, s);
+}
+
+}  // extern "C"

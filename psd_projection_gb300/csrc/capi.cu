@@ -504,7 +504,7 @@ uint64_t psdgb_kernel_launch_count(void) { return g_launches.load(); }
 
 int psdgb_set_product_config(int acc_mode) {
     const int prev = g_single_acc_mode;
-    if (acc_mode >= ACC_4X1 && acc_mode <= ACC_1X4) g_single_acc_mode = acc_mode;
+    if (acc_mode >= -1 && acc_mode <= ACC_1X4) g_single_acc_mode = acc_mode;
     return prev;
 }
 

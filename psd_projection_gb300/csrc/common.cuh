@@ -97,14 +97,15 @@ struct EpiParams {
 };
 
 // A group of independent blocks sharing one strided operand layout: block b
-// occupies layout rows [row_base, row_base + np) (row stride EpiParams::ld),
+// occupies layout rows [row_base, row_base + np) and columns [col_base,
+// col_base + np) (row stride EpiParams::ld),
 // its FP64 n x n matrix starts at element x_off of the packed input, and its
 // scale (for the final reconstruction) is *up_dev.
 struct BlockDesc {
     int row_base;
     int np;
     int n;
-    int pad;
+    int col_base;     // first layout column of the block (blocks share row bands)
     long long x_off;
     const double* up_dev;
 };

@@ -52,7 +52,8 @@ namespace {
 
 constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int TILE_BYTES = BM * BK * 2;  // one operand term tile: 128 rows x 128 bytes
-constexpr int THREADS = 192;
+constexpr int EPI_WARPS = 4;                   // one per TMEM lane quarter
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // producer warp, MMA warp, epilogue warps
 
 template <int TERMS>
 struct TcCfg {
@@ -103,7 +104,7 @@ __device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiPara
         ti.blk.row_base = 0;
         ti.blk.np = ep.np;
         ti.blk.n = ep.n;
-        ti.blk.pad = 0;
+        ti.blk.col_base = 0;
         ti.blk.x_off = 0;
         ti.blk.up_dev = ep.up_dev;
     }
@@ -117,16 +118,11 @@ __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag,
 
 // ---- epilogue helpers ------------------------------------------------------
 
-// Store 32 consecutive values of local row p (columns q0..q0+31) of a block
-// whose first layout row is rb, and their mirrors.  full: every element of
-// the run satisfies p > q (no diagonal masking).
+// Split 32 consecutive values and store them at element row_idx of every
+// term plane: 32 elements x 2 bytes per term = four 16-byte vectors.
 template <int FMT>
-__device__ __forceinline__ void store_run(const SplitMat& m, int64_t ld, int64_t rb, int64_t p, int64_t q0,
-                                          const float (&v)[32], bool full) {
+__device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, const float (&v)[32]) {
     constexpr int NT = FMT == FMT_F16 ? 2 : 3;
-    const size_t row_idx = static_cast<size_t>(rb + p) * ld + q0;
-    if (full) {
-        // Direct row store: 32 elements x 2 bytes per term = four 16-byte vectors.
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t packed[16];
@@ -158,16 +154,34 @@ __device__ __forceinline__ void store_run(const SplitMat& m, int64_t ld, int64_t
             for (int u = 0; u < 4; ++u)
                 dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
         }
+}
+
+// Store a 32 x 32 run of the warp (lane = local row p0 + lane, columns
+// q0..q0+31, every element strictly below the diagonal) and its mirror.  The
+// row is written as 16-byte vectors; the mirror (rows q0..q0+31, column
+// p0 + lane) element by element, which the warp's 32 lanes coalesce into
+// contiguous 64-byte stores.  (Transposing the mirror through shared memory
+// to write it as vectors measured 2-3 % slower.)
+template <int FMT>
+__device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p0,
+                                               int64_t q0, const float (&v)[32]) {
+    const int64_t p = p0 + (threadIdx.x & 31);
+    store_row32<FMT>(m, static_cast<size_t>(rb + p) * ld + cb + q0, v);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(rb + q0 + j) * ld + p, v[j]);
-    } else {
+    for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(rb + q0 + j) * ld + cb + p, v[j]);
+}
+
+// A run on the diagonal (q0 == p0): element-wise with the p >= q mask.
+template <int FMT>
+__device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p,
+                                               int64_t q0, const float (&v)[32]) {
+    const size_t row_idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-            const int64_t q = q0 + j;
-            if (p >= q) {
-                split_store(m, FMT, row_idx + j, v[j]);
-                if (p != q) split_store(m, FMT, static_cast<size_t>(rb + q) * ld + p, v[j]);
-            }
+    for (int j = 0; j < 32; ++j) {
+        const int64_t q = q0 + j;
+        if (p >= q) {
+            split_store(m, FMT, row_idx + j, v[j]);
+            if (p != q) split_store(m, FMT, static_cast<size_t>(rb + q) * ld + cb + p, v[j]);
         }
     }
 }
@@ -203,11 +217,14 @@ __device__ __forceinline__ void load_run(const SplitMat& m, size_t idx, float (&
     }
 }
 
-// Epilogue of one tile for the thread that owns local row p (tile rows bi).
+// Epilogue of one tile for the warp whose first local row is p0 (lane = row
+// p0 + lane).
 template <int FMT, int ACC_SPLIT>
-__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p, int nacc) {
+__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc) {
     const int64_t ld = ep.ld;
     const int64_t rb = ti.blk.row_base;
+    const int64_t cb = ti.blk.col_base;
+    const int64_t p = p0 + (threadIdx.x & 31);
     for (int c0 = 0; c0 < BN; c0 += 32) {
         float v[32];
         tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
@@ -221,7 +238,7 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
             }
         }
         const int64_t q0 = ti.bj * BN + c0;
-        if (q0 > p) continue;  // whole run above the diagonal: owned by the mirror tile
+        if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
         if (ep.kind == EPI_FINAL) {
             const int64_t n = ti.blk.n;
             if (p >= n) continue;
@@ -239,7 +256,7 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
             }
             continue;
         }
-        const size_t idx = static_cast<size_t>(rb + p) * ld + q0;
+        const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
         for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
         if (ep.kind == EPI_STEP) {
@@ -249,7 +266,10 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
 #pragma unroll
             for (int j = 0; j < 32; ++j) v[j] = fmaf(ep.c, v[j], fmaf(ep.b, a3[j], ep.a * a[j]));
         }
-        store_run<FMT>(ep.out, ld, rb, p, q0, v, p > q0 + 31);
+        if (q0 + 31 < p0)
+            store_run_full<FMT>(ep.out, ld, rb, cb, p0, q0, v);
+        else
+            store_run_diag<FMT>(ep.out, ld, rb, cb, p, q0, v);
     }
 }
 
@@ -288,7 +308,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int b = 0; b < ACC_BUFS; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], 4);  // one arrival per epilogue warp
+            mbar_init(&acc_empty[b], EPI_WARPS);  // one arrival per epilogue warp
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -318,6 +338,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int kb_total = kb_half * dual_mult;
             const int row_p = static_cast<int>(ti.blk.row_base + ti.bi * BM);
             const int row_q = static_cast<int>(ti.blk.row_base + ti.bj * BN);
+            const int col0 = ti.blk.col_base;
             for (int kb = 0; kb < kb_total; ++kb, ++g) {
                 const int s = g % STAGES;
                 const uint32_t ph = static_cast<uint32_t>(g / STAGES) & 1u;
@@ -336,7 +357,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const bool second = kb >= kb_half;
                 const CUtensorMap* mp = second ? tm.Q : tm.P;
                 const CUtensorMap* mq = second ? tm.P : tm.Q;
-                const int kx = (second ? kb - kb_half : kb) * BK;
+                const int kx = col0 + (second ? kb - kb_half : kb) * BK;
                 mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
 #pragma unroll
                 for (int t = 0; t < TERMS; ++t) tma_load_2d(st + t * TILE_BYTES, &mp[t], &full[s], kx, row_p);
@@ -405,14 +426,14 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             if (*abort_flag) break;
             tc_fence_after();
-            const int64_t p = ti.bi * BM + q4 * 32 + lane;
+            const int64_t p0 = ti.bi * BM + q4 * 32;
             const uint32_t tmem_row =
                 tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
             const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
             if (ep.fmt == FMT_F16)
-                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p, nacc);
+                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
             else
-                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p, nacc);
+                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -550,9 +571,23 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
     GroupWork gw{nullptr, nullptr};
     EpiParams e = ep;
     e.ld = static_cast<int>(np);
-    return gemm_tc_group(ds, precision, g_single_acc_mode, P, Q, np, np, e, gw, nt * (nt + 1) / 2, 0, s);
+    return gemm_tc_group(ds, precision, auto_acc_mode(precision, np), P, Q, np, np, e, gw, nt * (nt + 1) / 2, 0, s);
 }
 
-int g_single_acc_mode = ACC_4X1;
+int g_single_acc_mode = -1;
+
+// Accumulator configuration: the accuracy of one tensor-core FP32 accumulator
+// degrades with the number of K blocks it sums (n = 8192: 4.3e-5 rel. error
+// with one, 2.1e-5 with two, 1.1e-5 with four, for every split precision), so
+// long FP32-class products deal K over four accumulators; short ones, and the
+// one-term precisions (whose error is their operand rounding), double-buffer
+// the accumulators instead so the epilogue overlaps the next tile (+4-10 %).
+int auto_acc_mode(int precision, int64_t np) {
+    if (g_single_acc_mode >= 0) return g_single_acc_mode;
+    if (precision == PSDGB_PREC_FP16 || precision == PSDGB_PREC_BF16) return ACC_1X4;
+    if (np <= 2048) return ACC_1X4;
+    if (np <= 4096) return ACC_2X2;
+    return ACC_4X1;
+}
 
 }  // namespace psdgb

@@ -93,7 +93,8 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
 // interleaved accumulators (K/ACC_SPLIT additions each) x ACC_BUFS sets
 // (epilogue of one tile overlapping the next tile's MMAs); 512 TMEM columns.
 enum AccMode : int { ACC_4X1 = 0, ACC_2X2 = 1, ACC_1X4 = 2 };
-extern int g_single_acc_mode;  // configuration of the single-matrix products
+extern int g_single_acc_mode;  // forced configuration of single-matrix products, or -1 (automatic)
+int auto_acc_mode(int precision, int64_t np);
 // Grouped product over a tile list (see GroupWork), persistent over `grid`
 // CTAs (0: one per SM); operand planes of `rows` rows with row stride ld.
 psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "tridiag.cuh"
 
 namespace psdgb {
 
@@ -156,6 +157,7 @@ __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict_
         int64_t k = lane;
         while (k < ld4) {
             const int64_t kend = (k + 32 * 64 < ld4) ? k + 32 * 64 : ld4;
+#pragma unroll 8
             for (; k < kend; k += 32) {
                 const float4 a = __ldg(col + k);
                 const float4 b = xs4[k];
@@ -220,71 +222,7 @@ __global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzStat
     }
 }
 
-// ---- the tridiagonal eigenpair, on the device (one thread) ------------------
-
-// Number of eigenvalues of T strictly less than x (Sturm count of the LDL^T
-// pivots of T - x I).
-__device__ int64_t sturm_count(const double* d, const double* e, int64_t m, double x, double pivmin) {
-    int64_t cnt = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0) ++cnt;
-    for (int64_t i = 1; i < m; ++i) {
-        q = d[i] - x - e[i - 1] * e[i - 1] / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        if (q < 0) ++cnt;
-    }
-    return cnt;
-}
-
-// Solve (T - shift I) x = b in place by Gaussian elimination with partial
-// pivoting on the band (fill-in on a second superdiagonal); work holds 4m doubles.
-__device__ void tridiag_solve(const double* d, const double* e, int64_t m, double shift, double tiny, double* b,
-                              double* work) {
-    double* dl = work;
-    double* dd = work + m;
-    double* du = work + 2 * m;
-    double* du2 = work + 3 * m;
-    for (int64_t i = 0; i < m; ++i) {
-        dd[i] = d[i] - shift;
-        dl[i] = (i + 1 < m) ? e[i] : 0.0;
-        du[i] = (i + 1 < m) ? e[i] : 0.0;
-        du2[i] = 0.0;
-    }
-    for (int64_t i = 0; i + 1 < m; ++i) {
-        if (fabs(dd[i]) >= fabs(dl[i])) {
-            if (dd[i] == 0.0) dd[i] = tiny;
-            const double f = dl[i] / dd[i];
-            dd[i + 1] -= f * du[i];
-            b[i + 1] -= f * b[i];
-            dl[i] = 0.0;
-        } else {  // swap rows i and i+1
-            const double f = dd[i] / dl[i];
-            dd[i] = dl[i];
-            const double t = dd[i + 1];
-            dd[i + 1] = du[i] - f * t;
-            du[i] = t;
-            if (i + 2 < m) {
-                du2[i] = du[i + 1];
-                du[i + 1] = -f * du2[i];
-            }
-            const double tb = b[i];
-            b[i] = b[i + 1];
-            b[i + 1] = tb - f * b[i];
-        }
-    }
-    if (dd[m - 1] == 0.0) dd[m - 1] = tiny;
-    b[m - 1] /= dd[m - 1];
-    if (m > 1) b[m - 2] = (b[m - 2] - du[m - 2] * b[m - 1]) / dd[m - 2];
-    for (int64_t i = m - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) / dd[i];
-}
-
-// The reference forms T densely and takes the last eigenpair of cuSOLVER
-// Dsyevd (src/lanczos.cu:186-240).  Here one warp: theta by 33-way
-// multisection on the Sturm count (each lane evaluates one split point, a
-// ballot picks the sub-interval; about 11 rounds to full FP64 precision
-// instead of ~50 bisection steps of dependent FP64 divisions), then u by four
-// steps of inverse iteration in lane 0.
+// The largest eigenpair of T, by one warp (tridiag.cuh).
 __global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double* beta, double* uk, double* work) {
     const int lane = threadIdx.x;
     const int64_t m = st->nb_iter;
@@ -307,50 +245,10 @@ __global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double
         }
         return;
     }
-    const double* d = alpha;
-    const double* e = beta;
-    double lo = INFINITY, hi = -INFINITY, tnorm = 0.0;
-    for (int64_t i = 0; i < m; ++i) {
-        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < m ? fabs(e[i]) : 0.0);
-        lo = fmin(lo, d[i] - r);
-        hi = fmax(hi, d[i] + r);
-        tnorm = fmax(tnorm, fabs(d[i]) + r);
-    }
-    const double eps = 2.220446049250313e-16;
-    const double pivmin = fmax(2.2250738585072014e-308, eps * eps * tnorm * tnorm);
-    const double pad = 2.0 * eps * tnorm + pivmin;
-    lo -= pad;
-    hi += pad;
-    // Invariant: count(lo) < m <= count(hi); the largest eigenvalue lies in [lo, hi).
-    for (int it = 0; it < 64; ++it) {
-        if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
-        const double x = lo + (hi - lo) * (static_cast<double>(lane + 1) / 33.0);
-        const bool above = (x > lo && x < hi) ? (sturm_count(d, e, m, x, pivmin) >= m) : (x >= hi);
-        const unsigned mask = __ballot_sync(0xffffffffu, above);
-        const int first = mask ? __ffs(mask) - 1 : 32;  // first split point with all eigenvalues below it
-        const double new_hi = (first < 32) ? __shfl_sync(0xffffffffu, x, first) : hi;
-        const double new_lo = (first > 0) ? __shfl_sync(0xffffffffu, x, first > 0 ? first - 1 : 0) : lo;
-        if (!(new_hi < hi || new_lo > lo)) break;  // no progress at this precision
-        hi = new_hi;
-        lo = new_lo;
-    }
-    if (lane != 0) return;
-    st->no_ritz = 0;
-    const double t = 0.5 * (lo + hi);
-    st->theta = t;
-    const double tiny = eps * fmax(tnorm, 2.2250738585072014e-308);
-    const double shift = t + 4.0 * eps * fmax(tnorm, fabs(t));
-    for (int64_t i = 0; i < m; ++i) uk[i] = 1.0;
-    for (int it = 0; it < 4; ++it) {
-        tridiag_solve(d, e, m, shift, tiny, uk, work);
-        double s = 0.0;
-        for (int64_t i = 0; i < m; ++i) s += uk[i] * uk[i];
-        s = sqrt(s);
-        if (!(s > 0.0) || !isfinite(s)) {
-            for (int64_t i = 0; i < m; ++i) uk[i] = 1.0 / sqrt(static_cast<double>(m));
-            break;
-        }
-        for (int64_t i = 0; i < m; ++i) uk[i] /= s;
+    const double t = warp_tridiag_top(alpha, beta, m, uk, work);
+    if (lane == 0) {
+        st->no_ritz = 0;
+        st->theta = t;
     }
 }
 

@@ -1,0 +1,109 @@
+"""Block-diagonal batch: every block projected as by one call per block (GPU).
+
+Tolerances: batch vs one call per block 1e-5 relative Frobenius per block (the
+batch runs each block's Lanczos bound in one CTA with a different reduction
+order, so the scale differs in the last bits); each block within 1e-4 of the
+FP64 EVD projection (fp16x3).  Graph replay and the autotuned configuration
+reproduce the direct launch bit for bit.
+"""
+import numpy as np
+import pytest
+
+from oracle import reference_port as rp
+from tests.gpu_util import from_dev, to_dev
+
+pytestmark = pytest.mark.gpu
+
+
+def _blocks(sizes, seed):
+    """(G + G^T)/2 blocks; a 1 x 1 block is kept inside [-1, 1] because the
+    reference's Lanczos bound returns up = 1 for n = 1 (its first residual is
+    exactly zero), so a larger scalar would leave the filter's interval."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for n in sizes:
+        g = rng.standard_normal((n, n))
+        m = 0.5 * (g + g.T)
+        if n == 1:
+            m = np.array([[0.3]])
+        out.append(m)
+    return out
+
+
+SIZES = [1, 2, 16, 33, 64, 100, 127, 128, 129, 200, 256, 300, 384, 512, 17, 5, 480, 150, 90, 260]
+
+
+def test_batch_matches_one_call_per_block():
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    mats = _blocks(SIZES, seed=1)
+    d = pack(mats)
+    with BatchPlan(SIZES) as plan:
+        plan.project(d)
+        import torch
+
+        torch.cuda.synchronize()
+    got = unpack(d, SIZES)
+    for n, x, y in zip(SIZES, mats, got):
+        t = to_dev(x)
+        psd.composite_FP32_auto_scale(t)
+        one = from_dev(t)
+        assert rp.rel_frobenius(y, one) <= 1e-5 or np.linalg.norm(one) == 0.0, n
+        if n >= 2:
+            proj, _ = rp.eig_psd(x)
+            assert rp.rel_frobenius(y, proj) <= 1e-4, n
+
+
+def test_batch_graph_replay_and_autotune():
+    import torch
+
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    sizes = SIZES * 3
+    mats = _blocks(sizes, seed=2)
+    pristine = pack(mats)
+    with BatchPlan(sizes) as plan:
+        direct = pristine.clone()
+        plan.project(direct)
+        torch.cuda.synchronize()
+        scratch = pristine.clone()
+        plan.autotune(scratch)
+        tuned = pristine.clone()
+        plan.project(tuned)
+        work = pristine.clone()
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            plan.project(work.clone(), stream=side)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            plan.project(work)
+        work.copy_(pristine)
+        g.replay()
+        torch.cuda.synchronize()
+        info = plan.info()
+    a, b, c = unpack(direct, sizes), unpack(tuned, sizes), unpack(work, sizes)
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(y, z)
+        assert rp.rel_frobenius(x, y) <= 1e-6 or np.linalg.norm(x) == 0.0
+    assert info["num_tiles"] > 0
+
+
+def test_batch_bf16x9_and_fp16():
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    sizes = [64, 200, 130]
+    mats = _blocks(sizes, seed=3)
+    for prec, sched, tol in ((psd.PRECISIONS["bf16x9"], psd.SCHEDULE_FP32, 1e-4),
+                             (psd.PRECISIONS["fp16"], psd.SCHEDULE_FP16, 2e-3)):
+        d = pack(mats)
+        with BatchPlan(sizes, prec, sched) as plan:
+            plan.project(d)
+        got = unpack(d, sizes)
+        for x, y in zip(mats, got):
+            proj, _ = rp.eig_psd(x)
+            assert rp.rel_frobenius(y, proj) <= tol
