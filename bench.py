@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving session")
     ap.add_argument("--no-batch", action="store_true", help="skip the block-diagonal batch session")
     ap.add_argument("--only-batch", action="store_true", help="run only the block-diagonal batch session")
+    ap.add_argument("--only-configs", action="store_true", help="run only the n=1024 and n=16384 sessions")
+    ap.add_argument("--no-configs", action="store_true", help="skip the n=1024 and n=16384 sessions")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--workload", choices=["spectrum", "gaussian"], default="spectrum",
@@ -300,6 +302,102 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
 
 
 # ---------------------------------------------------------------------------
+# config 1 (n = 1024 Gaussian) and config 3 (n = 16384 precision stress)
+# ---------------------------------------------------------------------------
+
+def config1_session(n: int = 1024, seed: int = 0) -> dict:
+    """A = (G + G^T)/2, G ~ N(0,1) (seeded), stored FP32: composite_FP32 with
+    a 30-step Lanczos bound on the GPU against the FP64 LAPACK dsyevd
+    projection on the host; the relative Frobenius error between the two."""
+    import numpy as np
+    import torch
+
+    import psd_projection_gb300 as psd
+    from oracle import reference_port as rp
+
+    g = np.random.default_rng(seed).standard_normal((n, n))
+    x = (0.5 * (g + g.T)).astype(np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    proj, _ = rp.eig_psd(x)
+    cpu_s = time.perf_counter() - t0
+    d = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    work = d.clone()
+    psd.composite(work, max_iter=30)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    bufs = [d.clone() for _ in range(reps)]
+    e0.record()
+    for b in bufs:
+        psd.composite(b, max_iter=30)
+    e1.record()
+    torch.cuda.synchronize()
+    out = bufs[-1].cpu().numpy().T
+    return {"workload": "n=1024, A=(G+G^T)/2, G~N(0,1) seed 0, FP32 storage; composite_FP32 (fp16x3) with "
+                        "30 Lanczos steps vs host FP64 dsyevd projection",
+            "rel_frobenius_err": rp.rel_frobenius(out, proj), "gpu_ms": e0.elapsed_time(e1) / reps,
+            "cpu_dsyevd_s": cpu_s, "cpu_cores": os.cpu_count()}
+
+
+def config3_session(n: int = 16384, seed: int = 3) -> dict:
+    """Precision stress: Q diag(lambda) Q^T, Q from the QR of a seeded
+    Gaussian; 10% of lambda in |lambda| < 1e-3, 60% uniform in [-1, -1e-3],
+    30% uniform in [1e-3, 10]; stored FP32.  Each mode's error against the
+    exact projection Q diag(max(lambda, 0)) Q^T and its time."""
+    import torch
+
+    import psd_projection_gb300 as psd
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    t_setup = time.perf_counter()
+    G = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+    Q, _ = torch.linalg.qr(G)
+    del G
+    k1, k2 = n // 10, n // 10 + (6 * n) // 10
+    u = torch.rand(n, generator=g, dtype=torch.float64, device="cuda")
+    lam = torch.empty(n, dtype=torch.float64, device="cuda")
+    lam[:k1] = (u[:k1] * 2.0 - 1.0) * 1e-3
+    lam[k1:k2] = -1e-3 - u[k1:k2] * (1.0 - 1e-3)
+    lam[k2:] = 1e-3 + u[k2:] * (10.0 - 1e-3)
+    A = (Q * lam) @ Q.T
+    X = (0.5 * (A + A.T)).float().double()
+    del A
+    P = (Q * lam.clamp(min=0.0)) @ Q.T
+    P = 0.5 * (P + P.T)
+    del Q
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    runs = {}
+
+    def timed(name, fn):
+        t = X.clone()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn(t)
+        e1.record()
+        torch.cuda.synchronize()
+        runs[name] = {"ms": e0.elapsed_time(e1), "rel_frobenius_err": psd.rel_frobenius(t, P)}
+        del t
+
+    P16, P32 = psd.SCHEDULE_FP16, psd.SCHEDULE_FP32
+    timed("plain_fp32_simt", lambda t: psd.composite(t, psd.PRECISIONS["fp32_simt"], P32))
+    timed("fp16x3", lambda t: psd.composite(t, psd.PRECISIONS["fp16x3"], P32))
+    timed("bf16x9", lambda t: psd.composite(t, psd.PRECISIONS["bf16x9"], P32))
+    timed("bf16_bulk_only", lambda t: psd.composite(t, psd.PRECISIONS["bf16"], P16))
+    timed("fp16_bulk_only", lambda t: psd.composite(t, psd.PRECISIONS["fp16"], P16))
+    for r in (1, 2):
+        timed(f"bf16_bulk+{r}x_bf16x9_refine", lambda t, r=r: psd.composite_mixed(t, "bf16", "bf16x9", r))
+        timed(f"fp16_bulk+{r}x_fp16x3_refine", lambda t, r=r: psd.composite_mixed(t, "fp16", "fp16x3", r))
+    return {"workload": f"n={n} precision stress: 10% |lambda|<1e-3, 60% U[-1,-1e-3], 30% U[1e-3,10], "
+                        "Q=QR(N(0,1)) seed 3, FP32 storage; bulk = one-term products on the FP16 schedule, "
+                        "refinement = the FP32 table's final quintic in split precision",
+            "setup_s": setup_s, "runs": runs,
+            "note": "FP8 e4m3 bulk is not built; BF16 and FP16 one-term bulks stand in for it"}
+
+
+# ---------------------------------------------------------------------------
 # block-diagonal batch: 4096 uneven blocks
 # ---------------------------------------------------------------------------
 
@@ -536,6 +634,10 @@ def run_ours(args, rank, world):
     if not args.no_batch:
         out["batched"] = batched_session(count=args.batch_count)
 
+    if not args.no_configs:
+        out["config1"] = config1_session()
+        out["config3"] = config3_session()
+
     if not args.no_serve:
         sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
         out["serving"] = {
@@ -613,6 +715,9 @@ def main():
     rank, world = dist_setup()
     if args.only_batch:
         print(json.dumps({"batched": batched_session(count=args.batch_count)}))
+        return
+    if args.only_configs:
+        print(json.dumps({"config1": config1_session(), "config3": config3_session()}))
         return
     res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
     if rank == 0 and res is not None:

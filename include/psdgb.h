@@ -149,6 +149,14 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
                                               void* d_ws, size_t ws_bytes, void* d_lanczos,
                                               size_t lanczos_bytes, void* stream);
 
+/* Mixed precision (no counterpart in the reference): the Lanczos bound, the
+ * bulk_schedule's steps with bulk_precision products (one-term FP16 or BF16),
+ * then refine_steps steps of the quintic that ends the FP32 table (no safety
+ * factor) and the final reconstruction with refine_precision products
+ * (fp16x3 after fp16; bf16x3/x6/x9 after bf16 — the same operand format). */
+psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_schedule, int refine_precision,
+                                              int refine_steps, double* d_mat, int64_t n, void* stream);
+
 /* Synchronise the device and report (and clear) a device-side wait failure. */
 psdgb_status psdgb_check_device_error(void);
 

@@ -34,7 +34,7 @@ from ._capi import (DEFAULT_SEED, PREC_BF16, PREC_BF16X3, PREC_BF16X6, PREC_BF16
                     PsdgbError)
 
 __all__ = [
-    "composite", "composite_FP16", "composite_FP16_auto_scale", "composite_FP32", "composite_FP32_auto_scale",
+    "composite", "composite_mixed", "composite_FP16", "composite_FP16_auto_scale", "composite_FP32", "composite_FP32_auto_scale",
     "composite_FP32_emulated", "composite_FP32_emulated_auto_scale", "approximate_two_norm", "lanczos_details",
     "eig_FP64_psd", "eig_FP32_psd", "project", "project_host", "workspace_size", "filter_coefficients",
     "kernel_launch_count", "rel_frobenius", "PsdgbError", "PRECISIONS", "METHODS",
@@ -110,6 +110,17 @@ def composite(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, 
     st = lib.psdgb_composite(precision, schedule, ctypes.c_void_p(mat.data_ptr()), n, ws, wsb, _stream_ptr(stream))
     _capi.check(st, "psdgb_composite")
     return 1.0
+
+
+def composite_mixed(mat, bulk: str = "bf16", refine: str = "bf16x9", refine_steps: int = 2,
+                    bulk_schedule: int = SCHEDULE_FP16, stream=None) -> None:
+    """Low-precision bulk (one-term products) followed by refine_steps
+    FP32-class refinement steps and reconstruction, auto-scaled, in place."""
+    n = _check_mat(mat)
+    st = _capi.lib().psdgb_composite_mixed_auto_scale(PRECISIONS[bulk], bulk_schedule, PRECISIONS[refine],
+                                                      refine_steps, ctypes.c_void_p(mat.data_ptr()), n,
+                                                      _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite_mixed_auto_scale")
 
 
 def composite_FP16(mat, workspace=None):

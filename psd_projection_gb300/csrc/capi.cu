@@ -20,7 +20,8 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
                            void* lz_state, cudaStream_t s, double* up_out);
 psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                                bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
-                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out);
+                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out,
+                               int bulk_precision, int refine_steps);
 
 namespace {
 
@@ -388,7 +389,35 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
     PSDGB_TRY(device_state(&ds));
     PSDGB_TRY(require_sm103(ds));
     return composite_enqueue(ds, precision, schedule, d_mat, n, d_ws, true, max_iter, tol, seed, residual_mode,
-                             d_lanczos, static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out);
+                             d_lanczos, static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out, -1, 0);
+}
+
+psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_schedule, int refine_precision,
+                                              int refine_steps, double* d_mat, int64_t n, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    PrecisionInfo pb{}, pr{};
+    if (!precision_info(bulk_precision, &pb) || !precision_info(refine_precision, &pr) || pb.fmt != pr.fmt ||
+        refine_steps < 0 || refine_steps > 8) {
+        set_error("psdgb_composite_mixed_auto_scale: the bulk and refinement precisions must share an operand "
+                  "format (fp16 with fp16x3; bf16 with bf16x3/x6/x9) and 0 <= refine_steps <= 8");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (bulk_precision == PSDGB_PREC_BF16 && bulk_schedule != PSDGB_SCHEDULE_FP16) {
+        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n < 0 || (n > 0 && d_mat == nullptr)) { set_error("bad matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n == 0) return PSDGB_OK;
+    void *ws = nullptr, *lz = nullptr;
+    PSDGB_TRY(resolve_ws(ds, n, refine_precision, nullptr, 0, &ws));
+    PSDGB_TRY(resolve_lz(ds, n, 20, &lz));
+    PSDGB_TRY(composite_enqueue(ds, refine_precision, bulk_schedule, d_mat, n, ws, true, 20, 1e-10, kDefaultSeed,
+                                PSDGB_RESIDUAL_REFERENCE, lz, s, nullptr, nullptr, bulk_precision, refine_steps));
+    return finish(ds, s);
 }
 
 psdgb_status psdgb_check_device_error(void) {

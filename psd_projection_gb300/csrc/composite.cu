@@ -118,7 +118,8 @@ EpiParams epi_base(const Layout& L, int64_t n) {
     return ep;
 }
 
-psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layout& L, int64_t n, cudaStream_t s) {
+// One filter step A <- a A + b A^3 + c A^5 (three products) at a precision.
+psdgb_status run_step(DeviceState* ds, int precision, const Step& st, const Layout& L, int64_t n, cudaStream_t s) {
     PrecisionInfo pi{};
     precision_info(precision, &pi);
     // One-term operands round to 11 (FP16) or 8 (BF16) bits; the antisymmetric
@@ -126,7 +127,7 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
     // the symmetric part (A3*A2 + A2*A3)/2 as one dual product, as the
     // reference symmetrises A after every step (src/composite_FP16.cu:166).
     const bool dual_step = pi.nprod == 1;
-    for (const Step& st : schedule_steps(schedule)) {
+    {
         EpiParams e1 = epi_base(L, n);
         e1.kind = EPI_STORE;
         e1.out = L.A2;
@@ -148,6 +149,21 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
             e3.acc_scale = 0.5f;
         }
         PSDGB_TRY(gemm_symmetric(ds, precision, L.A3, L.A2, L.np, e3, s));  // A = aA + bA3 + cA3*A2
+    }
+    return PSDGB_OK;
+}
+
+// The whole schedule at one precision; or, with bulk_precision >= 0, the
+// schedule at bulk_precision followed by refine_steps steps of the
+// Newton-Schulz-type quintic that ends the FP32 table (no safety factor) at
+// `precision` — a low-precision bulk with higher-precision refinement.
+psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layout& L, int64_t n, cudaStream_t s,
+                        int bulk_precision = -1, int refine_steps = 0) {
+    const int bulk = bulk_precision >= 0 ? bulk_precision : precision;
+    for (const Step& st : schedule_steps(schedule)) PSDGB_TRY(run_step(ds, bulk, st, L, n, s));
+    if (bulk_precision >= 0) {
+        const Step fin = schedule_steps(PSDGB_SCHEDULE_FP32).back();
+        for (int r = 0; r < refine_steps; ++r) PSDGB_TRY(run_step(ds, precision, fin, L, n, s));
     }
     return PSDGB_OK;
 }
@@ -223,7 +239,8 @@ size_t composite_ws_bytes(int64_t n, int precision) {
 
 psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                                bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
-                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out) {
+                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out,
+                               int bulk_precision, int refine_steps) {
     PSDGB_TRY(check_n(n));
     PrecisionInfo pi{};
     if (!precision_info(precision, &pi)) {
@@ -257,7 +274,7 @@ psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, dou
     } else {
         PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, nullptr, L.A, L.fmt, L.np, s));
     }
-    PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s));
+    PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s, bulk_precision, refine_steps));
     PSDGB_TRY(run_final(ds, precision, L, mat, n, up_dev, inv_up_dev, s));
     return PSDGB_OK;
 }
@@ -267,7 +284,7 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
                            void* lz_state, cudaStream_t s, double* up_out) {
     if (up_out) *up_out = 1.0;
     PSDGB_TRY(composite_enqueue(ds, precision, schedule, mat, n, ws, auto_scale, max_iter, tol, seed, residual_mode,
-                                lz_state, s, nullptr, nullptr));
+                                lz_state, s, nullptr, nullptr, -1, 0));
     if (up_out && auto_scale && n > 0) {
         LanczosResult lr;
         PSDGB_TRY(lanczos_read(lz_state, n, max_iter, s, &lr, nullptr, nullptr));

@@ -249,3 +249,17 @@ def test_async_path_captures_in_a_cuda_graph(psd):
         g.replay()
         torch.cuda.synchronize()
         assert np.array_equal(from_dev(static_in), want)
+
+
+def test_mixed_bulk_and_refinement(psd):
+    """Low-precision bulk + split-precision refinement: valid and bounded."""
+    x = uniform_spectrum(300, 3.0, seed=31)
+    proj, _ = rp.eig_psd(x)
+    t = to_dev(x)
+    psd.composite_mixed(t, "fp16", "fp16x3", 2)
+    assert rp.rel_frobenius(from_dev(t), proj) <= 3e-3
+    t = to_dev(x)
+    psd.composite_mixed(t, "bf16", "bf16x9", 1)
+    assert rp.rel_frobenius(from_dev(t), proj) <= 3e-2
+    with pytest.raises(psd.PsdgbError, match="operand format"):
+        psd.composite_mixed(to_dev(x), "fp16", "bf16x9", 1)
