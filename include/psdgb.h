@@ -268,6 +268,24 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, 
  * tile overlaps the next tile's MMAs), 2 = one accumulator, four buffers.
  * Returns the previous value. */
 int psdgb_set_product_config(int acc_mode);
+/* Other product-kernel settings, process-wide; returns the previous value
+ * (-1 for an unknown knob; out-of-range values are ignored):
+ *   PSDGB_TUNE_TILE_GROUP  tile order of single-matrix products: the lower
+ *                          tiles are walked in groups of this many tile rows,
+ *                          column by column within a group (0 = row by row),
+ *                          which sets how many operand row blocks the tiles
+ *                          running at the same time share in L2; 0..64;
+ *   PSDGB_TUNE_TILE_SHAPE  tile of single-matrix products: -1 = automatic
+ *                          (default: 128 x 256 for one- and two-term
+ *                          precisions at n > 1920, else 128 x 128); 0 = one
+ *                          CTA per 128 x 128 tile; 1 = a CTA pair per
+ *                          256 x 128 tile (one tcgen05 MMA over two SMs, each
+ *                          supplying half of the B operand); 2 = one CTA per
+ *                          128 x 256 tile, K accumulated in chunks summed in
+ *                          FP32 registers (one- and two-term precisions; the
+ *                          three-term ones keep 128 x 128). */
+enum { PSDGB_TUNE_TILE_GROUP = 1, PSDGB_TUNE_TILE_SHAPE = 2 };
+int psdgb_set_product_tuning(int knob, int value);
 
 /* Product-kernel timing: when enabled, the library records a CUDA event pair
  * on the caller's stream around every filter-product launch and adds the

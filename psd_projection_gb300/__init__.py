@@ -249,3 +249,19 @@ def rel_frobenius(a, b, stream=None) -> float:
                                          ctypes.byref(out), _stream_ptr(stream))
     _capi.check(st, "psdgb_rel_frobenius")
     return out.value
+
+
+TUNE_TILE_GROUP = 1
+TUNE_TILE_SHAPE = 2
+TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256 = -1, 0, 1, 2
+
+
+def set_product_config(acc_mode: int) -> int:
+    """Accumulator configuration of single-matrix products (-1 automatic, 0, 1, 2); returns the previous one."""
+    return int(_capi.lib().psdgb_set_product_config(int(acc_mode)))
+
+
+def set_product_tuning(knob: int, value: int) -> int:
+    """TUNE_TILE_GROUP (tile rows per group of the tile order, 0 = row by row) or TUNE_TILE_SHAPE
+    (TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256); returns the previous value."""
+    return int(_capi.lib().psdgb_set_product_tuning(int(knob), int(value)))

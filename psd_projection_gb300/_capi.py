@@ -83,6 +83,7 @@ SIGNATURES = {
                                                  c_vp, c_size, c_vp, c_size, c_vp]),
     "psdgb_check_device_error": (c_int, []),
     "psdgb_set_product_config": (c_int, [c_int]),
+    "psdgb_set_product_tuning": (c_int, [c_int, c_int]),
     "psdgb_composite_mixed_auto_scale": (c_int, [c_int, c_int, c_int, c_int, c_vp, c_i64, c_vp]),
     "psdgb_composite_auto_scale": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_u64, c_int, c_vp, c_size,
                                            c_vp, P_dbl]),

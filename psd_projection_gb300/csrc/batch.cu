@@ -369,7 +369,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     PrecisionInfo pi{};
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
-    GroupWork gw{b->tiles[b->order], b->blocks};
+    GroupWork gw{b->tiles[b->order], b->blocks, 0};
     float coeffs[64];
     const int steps = psdgb_filter_coefficients(b->schedule, coeffs, 21);
     auto base = [&]() {

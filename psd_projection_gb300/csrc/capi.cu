@@ -537,6 +537,22 @@ int psdgb_set_product_config(int acc_mode) {
     return prev;
 }
 
+int psdgb_set_product_tuning(int knob, int value) {
+    switch (knob) {
+        case PSDGB_TUNE_TILE_GROUP: {
+            const int prev = g_tile_group_rows;
+            if (value >= 0 && value <= 64) g_tile_group_rows = value;
+            return prev;
+        }
+        case PSDGB_TUNE_TILE_SHAPE: {
+            const int prev = g_tile_shape;
+            if (value >= -1 && value <= TILE_WIDE_128X256) g_tile_shape = value;
+            return prev;
+        }
+        default: return -1;
+    }
+}
+
 psdgb_status psdgb_product_timing_enable(int on) {
     product_timing_collect();
     std::lock_guard<std::mutex> lk(g_timing_mu);

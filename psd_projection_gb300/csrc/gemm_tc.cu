@@ -38,240 +38,13 @@
 //
 // Every mbarrier wait is bounded (common.cuh); a wait that gives up records a
 // DeviceError, drains the copies and MMAs it issued, frees TMEM and returns.
-#include <cuda.h>
-#include <cudaTypedefs.h>
-
 #include <mutex>
 
-#include "epilogue.cuh"
-#include "internal.h"
+#include "tc_kernel.cuh"
 
 namespace psdgb {
 
 namespace {
-
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int TILE_BYTES = BM * BK * 2;  // one operand term tile: 128 rows x 128 bytes
-constexpr int EPI_WARPS = 4;                   // one per TMEM lane quarter
-constexpr int THREADS = 64 + 32 * EPI_WARPS;  // producer warp, MMA warp, epilogue warps
-
-template <int TERMS>
-struct TcCfg {
-    static constexpr int STAGES = TERMS == 1 ? 6 : (TERMS == 2 ? 3 : 2);
-    static constexpr int STAGE_BYTES = 2 * TERMS * TILE_BYTES;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 512 /*barriers*/;
-};
-
-struct alignas(64) TmapSet {
-    CUtensorMap P[3];
-    CUtensorMap Q[3];
-};
-
-// Term product list: product i multiplies term prod_a(i) of P by term
-// prod_b(i) of Q.  The first 1 / 3 / 6 / 9 products are the x1 / x3 / x6 / x9
-// schemes: (0,0); (0,1), (1,0); (0,2), (2,0), (1,1); (1,2), (2,1), (2,2).
-__host__ __device__ constexpr int prod_a(int i) {
-    return i == 2 ? 1 : i == 4 ? 2 : i == 5 ? 1 : i == 6 ? 1 : i == 7 ? 2 : i == 8 ? 2 : 0;
-}
-__host__ __device__ constexpr int prod_b(int i) {
-    return i == 1 ? 1 : i == 3 ? 2 : i == 5 ? 1 : i == 6 ? 2 : i == 7 ? 1 : i == 8 ? 2 : 0;
-}
-
-__device__ __forceinline__ void tri_decode(int64_t t, int64_t& bi, int64_t& bj) {
-    int64_t i = static_cast<int64_t>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
-    while ((i + 1) * (i + 2) / 2 <= t) ++i;
-    while (i * (i + 1) / 2 > t) --i;
-    bi = i;
-    bj = t - i * (i + 1) / 2;
-}
-
-struct TileInfo {
-    int64_t bi, bj;
-    BlockDesc blk;
-};
-
-// Tile t of the work list: from the device tables, or (tables == null) the
-// lower tiles of one block described by the epilogue parameters.
-__device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiParams& ep, int t) {
-    TileInfo ti;
-    if (gw.tiles != nullptr) {
-        const TileDesc td = gw.tiles[t];
-        ti.bi = td.bi;
-        ti.bj = td.bj;
-        ti.blk = gw.blocks[td.block];
-    } else {
-        tri_decode(t, ti.bi, ti.bj);
-        ti.blk.row_base = 0;
-        ti.blk.np = ep.np;
-        ti.blk.n = ep.n;
-        ti.blk.col_base = 0;
-        ti.blk.x_off = 0;
-        ti.blk.up_dev = ep.up_dev;
-    }
-    return ti;
-}
-
-__device__ __forceinline__ void record_error(int* err, volatile int* abort_flag, int code) {
-    *abort_flag = 1;
-    atomicCAS(err, 0, code);
-}
-
-// ---- epilogue helpers ------------------------------------------------------
-
-// Split 32 consecutive values and store them at element row_idx of every
-// term plane: 32 elements x 2 bytes per term = four 16-byte vectors.
-template <int FMT>
-__device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, const float (&v)[32]) {
-    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
-#pragma unroll
-        for (int t = 0; t < NT; ++t) {
-            uint32_t packed[16];
-            // Recompute the term t of each element (cheap; keeps registers low).
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-                float x0 = v[j], x1 = v[j + 1];
-                uint16_t h0 = 0, h1 = 0;
-#pragma unroll
-                for (int u = 0; u <= t; ++u) {
-                    if (FMT == FMT_F16) {
-                        __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
-                        h0 = __half_as_ushort(a0);
-                        h1 = __half_as_ushort(a1);
-                        x0 -= __half2float(a0);
-                        x1 -= __half2float(a1);
-                    } else {
-                        __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
-                        h0 = __bfloat16_as_ushort(a0);
-                        h1 = __bfloat16_as_ushort(a1);
-                        x0 -= __bfloat162float(a0);
-                        x1 -= __bfloat162float(a1);
-                    }
-                }
-                packed[j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
-            }
-            uint4* dst = reinterpret_cast<uint4*>(static_cast<uint16_t*>(m.term[t]) + row_idx);
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
-        }
-}
-
-// Store a 32 x 32 run of the warp (lane = local row p0 + lane, columns
-// q0..q0+31, every element strictly below the diagonal) and its mirror.  The
-// row is written as 16-byte vectors; the mirror (rows q0..q0+31, column
-// p0 + lane) element by element, which the warp's 32 lanes coalesce into
-// contiguous 64-byte stores.  (Transposing the mirror through shared memory
-// to write it as vectors measured 2-3 % slower.)
-template <int FMT>
-__device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p0,
-                                               int64_t q0, const float (&v)[32]) {
-    const int64_t p = p0 + (threadIdx.x & 31);
-    store_row32<FMT>(m, static_cast<size_t>(rb + p) * ld + cb + q0, v);
-#pragma unroll
-    for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(rb + q0 + j) * ld + cb + p, v[j]);
-}
-
-// A run on the diagonal (q0 == p0): element-wise with the p >= q mask.
-template <int FMT>
-__device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p,
-                                               int64_t q0, const float (&v)[32]) {
-    const size_t row_idx = static_cast<size_t>(rb + p) * ld + cb + q0;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const int64_t q = q0 + j;
-        if (p >= q) {
-            split_store(m, FMT, row_idx + j, v[j]);
-            if (p != q) split_store(m, FMT, static_cast<size_t>(rb + q) * ld + cb + p, v[j]);
-        }
-    }
-}
-
-template <int FMT>
-__device__ __forceinline__ void load_run(const SplitMat& m, size_t idx, float (&out)[32]) {
-    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
-#pragma unroll
-    for (int j = 0; j < 32; ++j) out[j] = 0.f;
-    // Sum the terms from the smallest to the largest.
-#pragma unroll
-    for (int t = NT - 1; t >= 0; --t) {
-        const uint4* src = reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(m.term[t]) + idx);
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const uint4 w = src[u];
-            const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                const uint16_t lo = static_cast<uint16_t>(ws[h] & 0xFFFFu), hi = static_cast<uint16_t>(ws[h] >> 16);
-                float f0, f1;
-                if (FMT == FMT_F16) {
-                    f0 = __half2float(__ushort_as_half(lo));
-                    f1 = __half2float(__ushort_as_half(hi));
-                } else {
-                    f0 = __bfloat162float(__ushort_as_bfloat16(lo));
-                    f1 = __bfloat162float(__ushort_as_bfloat16(hi));
-                }
-                out[8 * u + 2 * h] += f0;
-                out[8 * u + 2 * h + 1] += f1;
-            }
-        }
-    }
-}
-
-// Epilogue of one tile for the warp whose first local row is p0 (lane = row
-// p0 + lane).
-template <int FMT, int ACC_SPLIT>
-__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc) {
-    const int64_t ld = ep.ld;
-    const int64_t rb = ti.blk.row_base;
-    const int64_t cb = ti.blk.col_base;
-    const int64_t p = p0 + (threadIdx.x & 31);
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-        float v[32];
-        tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
-#pragma unroll
-        for (int a = 1; a < ACC_SPLIT; ++a) {
-            if (a < nacc) {
-                float w[32];
-                tmem_ld_32cols(tmem_row + static_cast<uint32_t>(a * BN + c0), w);
-#pragma unroll
-                for (int j = 0; j < 32; ++j) v[j] += w[j];
-            }
-        }
-        const int64_t q0 = ti.bj * BN + c0;
-        if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
-        if (ep.kind == EPI_FINAL) {
-            const int64_t n = ti.blk.n;
-            if (p >= n) continue;
-            const double up = ti.blk.up_dev ? ep.up * *ti.blk.up_dev : ep.up;
-            double* out = ep.out64 + ti.blk.x_off;
-            const double* x = ep.x64 + ti.blk.x_off;
-#pragma unroll
-            for (int j = 0; j < 32; ++j) {
-                const int64_t q = q0 + j;
-                if (q <= p && q < n) {
-                    const double o = 0.5 * (x[p * n + q] + up * static_cast<double>(ep.acc_scale * v[j]));
-                    out[p * n + q] = o;
-                    if (q != p) out[q * n + p] = o;
-                }
-            }
-            continue;
-        }
-        const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
-#pragma unroll
-        for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
-        if (ep.kind == EPI_STEP) {
-            float a[32], a3[32];
-            load_run<FMT>(ep.A, idx, a);
-            load_run<FMT>(ep.A3, idx, a3);
-#pragma unroll
-            for (int j = 0; j < 32; ++j) v[j] = fmaf(ep.c, v[j], fmaf(ep.b, a3[j], ep.a * a[j]));
-        }
-        if (q0 + 31 < p0)
-            store_run_full<FMT>(ep.out, ld, rb, cb, p0, q0, v);
-        else
-            store_run_diag<FMT>(ep.out, ld, rb, cb, p, q0, v);
-    }
-}
 
 // ---- the kernel --------------------------------------------------------------
 
@@ -469,36 +242,6 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 // ---- host side -------------------------------------------------------------
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    });
-    return fn;
-}
-
-// Tensor map over a row-major plane of `rows` rows with row stride ld (both
-// in elements; the inner extent is ld).
-bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16) {
-    auto fn = encode_fn();
-    if (!fn) return false;
-    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ld), static_cast<cuuint64_t>(rows)};
-    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
-    const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(BM)};
-    const cuuint32_t estr[2] = {1, 1};
-    const CUresult r =
-        fn(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box,
-           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
 template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS>
 psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
@@ -513,7 +256,7 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
     for (int t = 0; t < 3; ++t) {
         void* pb = (t < TERMS) ? P.term[t] : P.term[0];
         void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
-        if (!make_tmap(&tm.P[t], pb, ld, rows, BF16) || !make_tmap(&tm.Q[t], qb, ld, rows, BF16)) {
+        if (!make_tmap(&tm.P[t], pb, ld, rows, BF16, BM) || !make_tmap(&tm.Q[t], qb, ld, rows, BF16, BM)) {
             set_error("cuTensorMapEncodeTiled failed");
             return PSDGB_ERR_CUDA;
         }
@@ -544,6 +287,34 @@ psdgb_status launch_acc(DeviceState* ds, int acc_mode, const SplitMat& P, const 
 
 }  // namespace
 
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16, int box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ld), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 2};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(BK), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r =
+        fn(tm, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, base, dims, strides, box,
+           estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
                            int64_t ld, int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles,
                            int grid, cudaStream_t s) {
@@ -568,13 +339,20 @@ psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const S
 psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                      const EpiParams& ep, cudaStream_t s) {
     const int64_t nt = np / BM;
-    GroupWork gw{nullptr, nullptr};
     EpiParams e = ep;
     e.ld = static_cast<int>(np);
+    const bool three_terms = precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9;
+    int shape = g_tile_shape;
+    if (shape < 0) shape = (!three_terms && np >= 2048) ? TILE_WIDE_128X256 : TILE_128X128;
+    if (nt >= 2 && shape == TILE_PAIR_256X128)
+        return gemm_tc_pair(ds, precision, auto_acc_mode(precision, np), P, Q, np, e, s);
+    if (nt >= 2 && shape == TILE_WIDE_128X256 && !three_terms) return gemm_tc_wide(ds, precision, P, Q, np, e, s);
+    GroupWork gw{nullptr, nullptr, g_tile_group_rows};
     return gemm_tc_group(ds, precision, auto_acc_mode(precision, np), P, Q, np, np, e, gw, nt * (nt + 1) / 2, 0, s);
 }
 
 int g_single_acc_mode = -1;
+int g_tile_group_rows = 8;
 
 // Accumulator configuration: the accuracy of one tensor-core FP32 accumulator
 // degrades with the number of K blocks it sums (n = 8192: 4.3e-5 rel. error

@@ -95,6 +95,20 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
 enum AccMode : int { ACC_4X1 = 0, ACC_2X2 = 1, ACC_1X4 = 2 };
 extern int g_single_acc_mode;  // forced configuration of single-matrix products, or -1 (automatic)
 int auto_acc_mode(int precision, int64_t np);
+// Tile shape of single-matrix products: one CTA per 128 x 128 tile (gemm_tc.cu),
+// a CTA pair per 256 x 128 tile (gemm_tc2.cu), one CTA per 128 x 256 tile
+// (gemm_wide.cu; one- and two-term precisions, others use 128 x 128); -1
+// chooses: 128 x 256 for one- and two-term precisions at np >= 2048.
+enum TileShape : int { TILE_128X128 = 0, TILE_PAIR_256X128 = 1, TILE_WIDE_128X256 = 2 };
+extern int g_tile_shape;
+extern int g_tile_group_rows;  // tile order of single-matrix products (grouped_decode), 0 = row by row
+// One matrix on CTA pairs (gemm_tc2.cu): 256 x 128 tiles, one
+// tcgen05.mma.cta_group::2 per term product and K slice; np >= 256.
+psdgb_status gemm_tc_pair(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
+                          int64_t np, const EpiParams& ep, cudaStream_t s);
+// One matrix on 128 x 256 tiles (gemm_wide.cu): one- and two-term precisions; np >= 256.
+psdgb_status gemm_tc_wide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                          const EpiParams& ep, cudaStream_t s);
 // Grouped product over a tile list (see GroupWork), persistent over `grid`
 // CTAs (0: one per SM); operand planes of `rows` rows with row stride ld.
 psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,

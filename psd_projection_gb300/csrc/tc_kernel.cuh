@@ -1,0 +1,293 @@
+// tc_kernel.cuh — pieces shared by the tensor-core product kernels
+// (gemm_tc.cu: one CTA per 128 x 128 tile; gemm_tc2.cu: a CTA pair per
+// 256 x 128 tile): tile geometry, tile-list decoding, tensor maps and the
+// epilogue that turns an FP32 accumulator tile into the next operand.
+#pragma once
+
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "epilogue.cuh"
+#include "internal.h"
+
+namespace psdgb {
+
+// Tensor map over a row-major plane of `rows` rows with row stride ld (both
+// in elements; the inner extent is ld), boxes of 64 columns x box_rows rows,
+// 128-byte swizzle (gemm_tc.cu).
+bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16, int box_rows);
+
+namespace {
+
+constexpr int BM = 128, BN = 128;
+constexpr int EPI_WARPS = 4;                   // one per TMEM lane quarter
+constexpr int THREADS = 64 + 32 * EPI_WARPS;  // producer warp, MMA warp, epilogue warps
+constexpr int SMEM_LIMIT = 232448;             // 227 KB of dynamic shared memory per CTA
+
+constexpr int BK = 64;                         // K block: 128-byte rows, 128-byte swizzle
+constexpr int TILE_BYTES = BM * BK * 2;          // one operand term tile of 128 rows
+constexpr int HALF_TILE_BYTES = TILE_BYTES / 2;  // 64 rows: one CTA's half of a pair's B operand
+
+// Single-CTA pipeline: per K block, TERMS term tiles of P (rows bi) and of Q
+// (rows bj); the ring takes as many stages as fit.
+template <int TERMS>
+struct TcCfg {
+    static constexpr int STAGE_BYTES = 2 * TERMS * TILE_BYTES;
+    static constexpr int STAGES_FIT = (SMEM_LIMIT - 1024 /*align*/ - 512 /*barriers*/) / STAGE_BYTES;
+    static constexpr int STAGES = STAGES_FIT > 12 ? 12 : STAGES_FIT;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;
+    static_assert(STAGES >= 2, "pipeline depth");
+};
+
+struct TmapSet {
+    CUtensorMap P[3];
+    CUtensorMap Q[3];
+};
+
+// Term product list: product i multiplies term prod_a(i) of P by term
+// prod_b(i) of Q.  The first 1 / 3 / 6 / 9 products are the x1 / x3 / x6 / x9
+// schemes: (0,0); (0,1), (1,0); (0,2), (2,0), (1,1); (1,2), (2,1), (2,2).
+__host__ __device__ constexpr int prod_a(int i) {
+    return i == 2 ? 1 : i == 4 ? 2 : i == 5 ? 1 : i == 6 ? 1 : i == 7 ? 2 : i == 8 ? 2 : 0;
+}
+__host__ __device__ constexpr int prod_b(int i) {
+    return i == 1 ? 1 : i == 3 ? 2 : i == 5 ? 1 : i == 6 ? 2 : i == 7 ? 1 : i == 8 ? 2 : 0;
+}
+
+__device__ __forceinline__ void tri_decode(int64_t t, int64_t& bi, int64_t& bj) {
+    int64_t i = static_cast<int64_t>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    bi = i;
+    bj = t - i * (i + 1) / 2;
+}
+
+// Tile t of the lower triangle of an nt x nt tile grid in grouped order: the
+// tile rows are taken G at a time and each group is walked column by column
+// (bj outer, the group's rows bi inner), so the tiles that run at the same
+// time (one wave = consecutive t) read G row blocks of P and about
+// wave / G row blocks of Q instead of a few rows of P and every column of Q.
+// Fewer distinct row blocks per wave keep more operand reads in L2.
+__device__ __forceinline__ void grouped_decode(int64_t t, int64_t nt, int64_t G, int64_t& bi, int64_t& bj) {
+    int64_t i, j;
+    tri_decode(t, i, j);  // the row-major triangle order and this one share the groups' index ranges
+    const int64_t r0 = (i / G) * G;
+    const int64_t h = (r0 + G < nt ? r0 + G : nt) - r0;
+    int64_t u = t - r0 * (r0 + 1) / 2;
+    if (u < r0 * h) {  // the full columns left of the group's own triangle
+        bj = u / h;
+        bi = r0 + u % h;
+        return;
+    }
+    u -= r0 * h;
+    int64_t c = 0;  // column c of the group's triangle holds h - c tiles
+    while (u >= h - c) {
+        u -= h - c;
+        ++c;
+    }
+    bj = r0 + c;
+    bi = bj + u;
+}
+
+struct TileInfo {
+    int64_t bi, bj;
+    BlockDesc blk;
+};
+
+// Tile t of the work list: from the device tables, or (tables == null) the
+// lower tiles of one block described by the epilogue parameters.
+__device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiParams& ep, int t) {
+    TileInfo ti;
+    if (gw.tiles != nullptr) {
+        const TileDesc td = gw.tiles[t];
+        ti.bi = td.bi;
+        ti.bj = td.bj;
+        ti.blk = gw.blocks[td.block];
+    } else {
+        if (gw.group_rows > 0)
+            grouped_decode(t, ep.np / BM, gw.group_rows, ti.bi, ti.bj);
+        else
+            tri_decode(t, ti.bi, ti.bj);
+        ti.blk.row_base = 0;
+        ti.blk.np = ep.np;
+        ti.blk.n = ep.n;
+        ti.blk.col_base = 0;
+        ti.blk.x_off = 0;
+        ti.blk.up_dev = ep.up_dev;
+    }
+    return ti;
+}
+
+__device__ __forceinline__ void record_error(int* err, volatile int* abort_flag, int code) {
+    *abort_flag = 1;
+    atomicCAS(err, 0, code);
+}
+
+// ---- epilogue helpers ------------------------------------------------------
+
+// Split 32 consecutive values and store them at element row_idx of every
+// term plane: 32 elements x 2 bytes per term = four 16-byte vectors.
+template <int FMT>
+__device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, const float (&v)[32]) {
+    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            uint32_t packed[16];
+            // Recompute the term t of each element (cheap; keeps registers low).
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                float x0 = v[j], x1 = v[j + 1];
+                uint16_t h0 = 0, h1 = 0;
+#pragma unroll
+                for (int u = 0; u <= t; ++u) {
+                    if (FMT == FMT_F16) {
+                        __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
+                        h0 = __half_as_ushort(a0);
+                        h1 = __half_as_ushort(a1);
+                        x0 -= __half2float(a0);
+                        x1 -= __half2float(a1);
+                    } else {
+                        __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
+                        h0 = __bfloat16_as_ushort(a0);
+                        h1 = __bfloat16_as_ushort(a1);
+                        x0 -= __bfloat162float(a0);
+                        x1 -= __bfloat162float(a1);
+                    }
+                }
+                packed[j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
+            }
+            uint4* dst = reinterpret_cast<uint4*>(static_cast<uint16_t*>(m.term[t]) + row_idx);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                dst[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+        }
+}
+
+// Store a 32 x 32 run of the warp (lane = local row p0 + lane, columns
+// q0..q0+31, every element strictly below the diagonal) and its mirror.  The
+// row is written as 16-byte vectors; the mirror (rows q0..q0+31, column
+// p0 + lane) element by element, which the warp's 32 lanes coalesce into
+// contiguous 64-byte stores.  (Transposing the mirror through shared memory
+// to write it as vectors measured 2-3 % slower.)
+template <int FMT>
+__device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p0,
+                                               int64_t q0, const float (&v)[32]) {
+    const int64_t p = p0 + (threadIdx.x & 31);
+    store_row32<FMT>(m, static_cast<size_t>(rb + p) * ld + cb + q0, v);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) split_store(m, FMT, static_cast<size_t>(rb + q0 + j) * ld + cb + p, v[j]);
+}
+
+// A run on the diagonal (q0 == p0): element-wise with the p >= q mask.
+template <int FMT>
+__device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p,
+                                               int64_t q0, const float (&v)[32]) {
+    const size_t row_idx = static_cast<size_t>(rb + p) * ld + cb + q0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+        const int64_t q = q0 + j;
+        if (p >= q) {
+            split_store(m, FMT, row_idx + j, v[j]);
+            if (p != q) split_store(m, FMT, static_cast<size_t>(rb + q) * ld + cb + p, v[j]);
+        }
+    }
+}
+
+// Eight consecutive values of a split matrix at element idx (one 16-byte
+// vector per term plane), the terms summed from the smallest to the largest.
+template <int FMT>
+__device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (&out)[8]) {
+    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) out[j] = 0.f;
+#pragma unroll
+    for (int t = NT - 1; t >= 0; --t) {
+        const uint4 w = *reinterpret_cast<const uint4*>(static_cast<const uint16_t*>(m.term[t]) + idx);
+        const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const uint16_t lo = static_cast<uint16_t>(ws[h] & 0xFFFFu), hi = static_cast<uint16_t>(ws[h] >> 16);
+            if (FMT == FMT_F16) {
+                out[2 * h] += __half2float(__ushort_as_half(lo));
+                out[2 * h + 1] += __half2float(__ushort_as_half(hi));
+            } else {
+                out[2 * h] += __bfloat162float(__ushort_as_bfloat16(lo));
+                out[2 * h + 1] += __bfloat162float(__ushort_as_bfloat16(hi));
+            }
+        }
+    }
+}
+
+// The epilogue of one 32 x 32 run of accumulator values v (lane = row
+// p0 + lane, columns q0 .. q0 + 31, q0 <= p0 + 31): the final reconstruction
+// in FP64, or the polynomial step / plain store with the operand split, at
+// (p, q) and at the mirror (q, p).
+template <int FMT>
+__device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo& ti, int64_t p0, int64_t q0,
+                                             float (&v)[32]) {
+    const int64_t ld = ep.ld;
+    const int64_t rb = ti.blk.row_base;
+    const int64_t cb = ti.blk.col_base;
+    const int64_t p = p0 + (threadIdx.x & 31);
+    if (ep.kind == EPI_FINAL) {
+        const int64_t n = ti.blk.n;
+        if (p >= n) return;
+        const double up = ti.blk.up_dev ? ep.up * *ti.blk.up_dev : ep.up;
+        double* out = ep.out64 + ti.blk.x_off;
+        const double* x = ep.x64 + ti.blk.x_off;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int64_t q = q0 + j;
+            if (q <= p && q < n) {
+                const double o = 0.5 * (x[p * n + q] + up * static_cast<double>(ep.acc_scale * v[j]));
+                out[p * n + q] = o;
+                if (q != p) out[q * n + p] = o;
+            }
+        }
+        return;
+    }
+    const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
+    if (ep.kind == EPI_STEP) {
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            float a[8], a3[8];
+            load_run8<FMT>(ep.A, idx + 8 * g, a);
+            load_run8<FMT>(ep.A3, idx + 8 * g, a3);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) v[8 * g + j] = fmaf(ep.c, v[8 * g + j], fmaf(ep.b, a3[j], ep.a * a[j]));
+        }
+    }
+    if (q0 + 31 < p0)
+        store_run_full<FMT>(ep.out, ld, rb, cb, p0, q0, v);
+    else
+        store_run_diag<FMT>(ep.out, ld, rb, cb, p, q0, v);
+}
+
+// Epilogue of one tile for the warp whose first local row is p0 (lane = row
+// p0 + lane), reading the accumulators from TMEM.  TN is the tile width (the
+// MMA's N): ti.bj counts column tiles of TN, and the ACC_SPLIT accumulators
+// of a tile sit TN TMEM columns apart.
+template <int FMT, int ACC_SPLIT, int TN = BN>
+__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc) {
+    for (int c0 = 0; c0 < TN; c0 += 32) {
+        float v[32];
+        tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
+#pragma unroll
+        for (int a = 1; a < ACC_SPLIT; ++a) {
+            if (a < nacc) {
+                float w[32];
+                tmem_ld_32cols(tmem_row + static_cast<uint32_t>(a * TN + c0), w);
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] += w[j];
+            }
+        }
+        const int64_t q0 = ti.bj * TN + c0;
+        if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
+        epilogue_run<FMT>(ep, ti, p0, q0, v);
+    }
+}
+
+}  // namespace
+}  // namespace psdgb

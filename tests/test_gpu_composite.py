@@ -263,3 +263,64 @@ def test_mixed_bulk_and_refinement(psd):
     assert rp.rel_frobenius(from_dev(t), proj) <= 3e-2
     with pytest.raises(psd.PsdgbError, match="operand format"):
         psd.composite_mixed(to_dev(x), "fp16", "bf16x9", 1)
+
+
+@pytest.mark.parametrize("precision", ["fp16x3", "bf16x9", "fp16", "bf16x6"])
+@pytest.mark.parametrize("n", [129, 300, 513, 1000])
+@pytest.mark.parametrize("acc_mode", [0, 1, 2])
+def test_pair_products_match_single_cta(psd, precision, n, acc_mode):
+    """Products on CTA pairs (256 x 128 tiles, one cta_group::2 MMA over two
+    SMs) and products with one CTA per 128 x 128 tile give the same projection
+    (same term products, same K order per accumulator): relative difference
+    <= 1e-6, and each within the FP32-class bar of the FP64 EVD projection."""
+    x = uniform_spectrum(n, 2.0, seed=40 + n)
+    proj, _ = rp.eig_psd(x)
+    prev_acc = psd.set_product_config(acc_mode)
+    prev_shape = psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_128X128)
+    try:
+        single, _ = run(psd, x, precision, auto_scale=True)
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_PAIR_256X128)
+        pair, _ = run(psd, x, precision, auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, prev_shape)
+        psd.set_product_config(prev_acc)
+    assert np.linalg.norm(pair - single) <= 1e-6 * np.linalg.norm(single)
+    bar = 2e-3 if precision == "fp16" else 1e-4
+    assert rp.rel_frobenius(pair, proj) <= bar
+
+
+@pytest.mark.parametrize("group", [0, 1, 3, 8])
+def test_tile_order_does_not_change_results(psd, group):
+    """The tile order (grouped raster) changes which CTA computes a tile, not its arithmetic: bit-identical."""
+    x = uniform_spectrum(700, 1.5, seed=77)
+    prev = psd.set_product_tuning(psd.TUNE_TILE_GROUP, 0)
+    try:
+        ref, _ = run(psd, x, "fp16x3", auto_scale=True)
+        psd.set_product_tuning(psd.TUNE_TILE_GROUP, group)
+        got, _ = run(psd, x, "fp16x3", auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_TILE_GROUP, prev)
+    assert np.array_equal(ref, got)
+
+
+@pytest.mark.parametrize("precision", ["fp16x3", "bf16x3", "fp16", "bf16"])
+@pytest.mark.parametrize("n", [129, 300, 513, 1000])
+def test_wide_tiles_match_oracle(psd, precision, n):
+    """128 x 256 tiles: within the bars of the FP64 EVD projection and close
+    to the 128 x 128 kernel.  The K order per accumulator differs, so the two
+    differ by about the precision's own error: <= 1e-5 for fp16x3, 5e-5 for
+    bf16x3 (1.8e-5 from the exact projection at n = 8192), 1e-3 for the
+    one-term products."""
+    x = uniform_spectrum(n, 2.0, seed=60 + n)
+    proj, _ = rp.eig_psd(x)
+    prev_shape = psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_128X128)
+    try:
+        ref, _ = run(psd, x, precision, auto_scale=True)
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_WIDE_128X256)
+        wide, _ = run(psd, x, precision, auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, prev_shape)
+    one_term = precision in ("fp16", "bf16")
+    diff_tol = {"fp16x3": 1e-5, "bf16x3": 5e-5}.get(precision, 1e-3)
+    assert np.linalg.norm(wide - ref) <= diff_tol * np.linalg.norm(ref)
+    assert rp.rel_frobenius(wide, proj) <= EVD_TOL.get(precision, 1e-4) * (2 if one_term else 1)
