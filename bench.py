@@ -42,6 +42,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "n=8192 proj/s & TC TFLOP/s vs plain FP32 at equal error; p50/p99 serve latency"
 
+# DRAM bytes (read + write) of one product launch, from one ncu capture of the
+# same kernel on the same workload size (profiles/ holds the summary).
+TRAFFIC_PER_LAUNCH = {(8192, "fp16x3", True): 2.015e9}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/tc_wide_kernel_fp16x3_n8192.md)"
+
 
 def parse_args():
     ap = argparse.ArgumentParser()
@@ -569,14 +574,23 @@ def run_ours(args, rank, world):
     per_launch_ms = pms.value / max(pl.value, 1)
     achieved = per_launch_flops / (per_launch_ms / 1e3) / 1e12 if pl.value else None
     peak = peaks["bf16_tflops_sustained"]
+    np_ = -(-n // 128) * 128
+    wide = args.precision in ("fp16", "bf16", "fp16x3", "bf16x3") and np_ >= 2048
+    kernel = (f"tc_wide_kernel (128x256 tiles, {args.precision} split operands, K chunks summed in FP32 registers)"
+              if wide else f"tc_group_kernel (128x128 tiles, {args.precision} split operands)")
     roofline = {
-        "bound": "tensor", "kernel": "tc_sym_kernel (symmetric product, fp16x3 split operands)",
+        "bound": "tensor", "kernel": kernel,
         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": (achieved / peak) if achieved else None,
         "peak_source": f"{peaks['source']} bf16_tflops_sustained (of {peaks['source']})",
+        "frac_of_burst": (achieved / peaks["bf16_tflops"]) if achieved and peaks.get("bf16_tflops") else None,
         "flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms, "launches": pl.value,
+        "flops_counted": "MMA flops of the lower-triangle 128x128 tiles: term products x 2 x 128 x 128 x K "
+                         "per tile (K doubled for the final dual product); the 1.5 % of above-diagonal work the "
+                         "128x256 tiles also do is not counted",
         "share_of_step": (pms.value / ms_total) if ms_total else None,
-        "traffic": None,
+        "traffic": TRAFFIC_PER_LAUNCH.get((n, args.precision, wide)),
+        "traffic_source": TRAFFIC_SOURCE if (n, args.precision, wide) in TRAFFIC_PER_LAUNCH else None,
     }
 
     out = {

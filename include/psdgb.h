@@ -283,8 +283,12 @@ int psdgb_set_product_config(int acc_mode);
  *                          supplying half of the B operand); 2 = one CTA per
  *                          128 x 256 tile, K accumulated in chunks summed in
  *                          FP32 registers (one- and two-term precisions; the
- *                          three-term ones keep 128 x 128). */
-enum { PSDGB_TUNE_TILE_GROUP = 1, PSDGB_TUNE_TILE_SHAPE = 2 };
+ *                          three-term ones keep 128 x 128);
+ *   PSDGB_TUNE_WIDE_KBLOCK K block of a pipeline stage of the 128 x 256 tiles:
+ *                          0 = by precision (default: 32 for two-term, 64 for
+ *                          one-term products), 64 (128-byte rows) or 32
+ *                          (64-byte rows, twice the stages). */
+enum { PSDGB_TUNE_TILE_GROUP = 1, PSDGB_TUNE_TILE_SHAPE = 2, PSDGB_TUNE_WIDE_KBLOCK = 3 };
 int psdgb_set_product_tuning(int knob, int value);
 
 /* Product-kernel timing: when enabled, the library records a CUDA event pair

@@ -549,6 +549,11 @@ int psdgb_set_product_tuning(int knob, int value) {
             if (value >= -1 && value <= TILE_WIDE_128X256) g_tile_shape = value;
             return prev;
         }
+        case PSDGB_TUNE_WIDE_KBLOCK: {
+            const int prev = g_wide_kblock;
+            if (value == 0 || value == 32 || value == 64) g_wide_kblock = value;
+            return prev;
+        }
         default: return -1;
     }
 }

@@ -355,6 +355,18 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
     return d;
 }
 
+// The same for 64-byte rows (K blocks of 32 FP16 / BF16) with the 64-byte
+// swizzle: 8-row groups 512 bytes apart, swizzle mode 4.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
+    d |= static_cast<uint64_t>(1u) << 16;
+    d |= static_cast<uint64_t>(512u >> 4) << 32;
+    d |= static_cast<uint64_t>(1u) << 46;
+    d |= static_cast<uint64_t>(4u) << 61;
+    return d;
+}
+
 #endif  // __CUDACC__
 
 // Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator

@@ -101,6 +101,7 @@ int auto_acc_mode(int precision, int64_t np);
 // chooses: 128 x 256 for one- and two-term precisions at np >= 2048.
 enum TileShape : int { TILE_128X128 = 0, TILE_PAIR_256X128 = 1, TILE_WIDE_128X256 = 2 };
 extern int g_tile_shape;
+extern int g_wide_kblock;  // K block of the 128 x 256 kernel: 64, 32, or 0 (by precision)
 extern int g_tile_group_rows;  // tile order of single-matrix products (grouped_decode), 0 = row by row
 // One matrix on CTA pairs (gemm_tc2.cu): 256 x 128 tiles, one
 // tcgen05.mma.cta_group::2 per term product and K slice; np >= 256.

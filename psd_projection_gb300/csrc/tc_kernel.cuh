@@ -13,9 +13,10 @@
 namespace psdgb {
 
 // Tensor map over a row-major plane of `rows` rows with row stride ld (both
-// in elements; the inner extent is ld), boxes of 64 columns x box_rows rows,
-// 128-byte swizzle (gemm_tc.cu).
-bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16, int box_rows);
+// in elements; the inner extent is ld), boxes of box_cols columns x box_rows
+// rows: 64 columns (128-byte rows) with the 128-byte swizzle, 32 columns
+// (64-byte rows) with the 64-byte swizzle (gemm_tc.cu).
+bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16, int box_rows, int box_cols = 64);
 
 namespace {
 

@@ -324,3 +324,22 @@ def test_wide_tiles_match_oracle(psd, precision, n):
     diff_tol = {"fp16x3": 1e-5, "bf16x3": 5e-5}.get(precision, 1e-3)
     assert np.linalg.norm(wide - ref) <= diff_tol * np.linalg.norm(ref)
     assert rp.rel_frobenius(wide, proj) <= EVD_TOL.get(precision, 1e-4) * (2 if one_term else 1)
+
+
+@pytest.mark.parametrize("precision", ["fp16x3", "bf16x3", "fp16"])
+def test_default_large_path_matches_evd(psd, precision):
+    """n = 2100 takes the automatic large-matrix path (128 x 256 tiles, K in
+    register-summed chunks): within the bars of the FP64 EVD projection, and
+    the 32- and 64-wide K blocks agree."""
+    x = uniform_spectrum(2100, 1.0, seed=9)
+    proj, _ = rp.eig_psd(x)
+    out, _ = run(psd, x, precision, auto_scale=True)
+    # One-term FP16 products lose accuracy with n (1.4e-3 here, 1.25e-3 at
+    # n = 8192, on either tile shape): its bar at this size is 2e-3.
+    assert rp.rel_frobenius(out, proj) <= (2e-3 if precision == "fp16" else 1e-4)
+    prev = psd.set_product_tuning(psd.TUNE_WIDE_KBLOCK, 64 if precision != "fp16" else 32)
+    try:
+        other, _ = run(psd, x, precision, auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_WIDE_KBLOCK, prev)
+    assert np.linalg.norm(other - out) <= (1e-3 if precision == "fp16" else 2e-5) * np.linalg.norm(out)
