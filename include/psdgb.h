@@ -260,6 +260,20 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
 
+/* A sequence of `count` n x n host matrices (h_in[i] -> h_out[i]; a buffer
+ * may appear more than once and h_out[i] may equal h_in[i], but h_out[i] must
+ * not be h_in[i + 1], which is read while matrix i is projected) with one
+ * method, pipelined: the host-to-device copy of matrix i + 1 and the
+ * device-to-host copy of matrix i - 1 run on their own streams while matrix i
+ * is projected on `stream`, through two device staging matrices.  Copies
+ * overlap only for page-locked host buffers (cudaHostAlloc / cudaHostRegister).
+ * Returns after the last result is in host memory.  The EVD methods run the
+ * matrices one after the other.  No counterpart in the reference, whose
+ * MATLAB entry point (MATLAB/psd_projection_MATLAB.cu:93-166) projects one
+ * matrix per call. */
+psdgb_status psdgb_project_host_many(const char* method, const double* const* h_in, double* const* h_out, int64_t n,
+                                     int64_t count, void* stream);
+
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Accumulator configuration of the tensor-core products of single-matrix
  * calls: -1 = automatic (default: four interleaved K accumulators for long

@@ -236,6 +236,43 @@ def project_host(method: str, a, out=None, stream=None):
     return out, eigs
 
 
+def project_host_many(method: str, inputs, outputs, stream=None):
+    """Project a sequence of (n, n) float64 host matrices (numpy arrays or
+    pinned CPU tensors, column-major) with one method: inputs[i] -> outputs[i],
+    the copies of neighbouring matrices overlapping each projection
+    (psdgb_project_host_many).  outputs[i] must not be inputs[i + 1]."""
+    import numpy as np
+
+    torch = _torch()
+    if len(inputs) != len(outputs):
+        raise ValueError("inputs and outputs differ in length")
+    count = len(inputs)
+    if count == 0:
+        return outputs
+
+    def ptr(x):
+        if isinstance(x, torch.Tensor):
+            if x.dtype != torch.float64 or x.device.type != "cpu" or not x.is_contiguous():
+                raise ValueError("host tensors must be contiguous float64 CPU tensors")
+            return x.data_ptr(), x.shape
+        if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags.c_contiguous):
+            raise ValueError("host arrays must be C-contiguous float64")
+        return x.ctypes.data, x.shape
+
+    src = [ptr(x) for x in inputs]
+    dst = [ptr(x) for x in outputs]
+    n = src[0][1][0]
+    for p_, shape in src + dst:
+        if tuple(shape) != (n, n):
+            raise ValueError("all matrices must be n x n with the same n")
+    arr_in = (ctypes.c_void_p * count)(*[p_ for p_, _ in src])
+    arr_out = (ctypes.c_void_p * count)(*[p_ for p_, _ in dst])
+    st = _capi.lib().psdgb_project_host_many(method.encode(), ctypes.cast(arr_in, ctypes.c_void_p),
+                                             ctypes.cast(arr_out, ctypes.c_void_p), n, count, _stream_ptr(stream))
+    _capi.check(st, "psdgb_project_host_many")
+    return outputs
+
+
 def kernel_launch_count() -> int:
     return int(_capi.lib().psdgb_kernel_launch_count())
 

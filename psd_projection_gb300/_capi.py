@@ -93,6 +93,7 @@ SIGNATURES = {
     "psdgb_eig_psd": (c_int, [c_int, c_vp, c_i64, c_vp, c_vp]),
     "psdgb_project": (c_int, [c_str, c_vp, c_i64, c_vp, c_vp]),
     "psdgb_project_host": (c_int, [c_str, c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "psdgb_project_host_many": (c_int, [c_str, c_vp, c_vp, c_i64, c_i64, c_vp]),
     "psdgb_kernel_launch_count": (c_u64, []),
     "psdgb_rel_frobenius": (c_int, [c_vp, c_vp, c_i64, P_dbl, c_vp]),
     "psdgb_filter_coefficients": (c_int, [c_int, ctypes.POINTER(ctypes.c_float), c_int]),

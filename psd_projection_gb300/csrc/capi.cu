@@ -529,6 +529,72 @@ psdgb_status psdgb_project_host(const char* method, const double* h_in, double* 
     return PSDGB_OK;
 }
 
+// A sequence of host matrices through one device: matrix i's host-to-device
+// copy, projection and device-to-host copy run on three streams ordered by
+// events, with two staging matrices, so the copies of matrices i + 1 and
+// i - 1 overlap the projection of matrix i.  Composite methods use the
+// asynchronous path (scale kept on the device); EVD methods run one matrix
+// after the other.
+psdgb_status psdgb_project_host_many(const char* method, const double* const* h_in, double* const* h_out, int64_t n,
+                                     int64_t count, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    int precision = 0, schedule = 0, eig64 = -1;
+    if (!method_precision(method, &precision, &schedule, &eig64)) {
+        set_error("Unknown method. Supported methods: 'composite_FP16', 'composite_FP32', "
+                  "'composite_FP32_emulated', 'eig_FP64', and 'eig_FP32'.");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n < 0 || count < 0) { set_error("bad matrix size or count"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n == 0 || count == 0) return PSDGB_OK;
+    if (!h_in || !h_out) { set_error("null host buffer list"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    for (int64_t i = 0; i < count; ++i)
+        if (!h_in[i] || !h_out[i]) { set_error("null host buffer"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (eig64 >= 0) {
+        for (int64_t i = 0; i < count; ++i) PSDGB_TRY(psdgb_project_host(method, h_in[i], h_out[i], n, nullptr, stream));
+        return PSDGB_OK;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (!ds->copy_in) {
+        PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&ds->copy_in, cudaStreamNonBlocking));
+        PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&ds->copy_out, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->in_done[b], cudaEventDisableTiming));
+            PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->comp_done[b], cudaEventDisableTiming));
+            PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->out_done[b], cudaEventDisableTiming));
+        }
+    }
+    const size_t bytes = sizeof(double) * static_cast<size_t>(n) * n;
+    const size_t stride = (bytes + 255) / 256 * 256;
+    PSDGB_TRY(ensure_buffer(&ds->stage2, &ds->stage2_bytes, 2 * stride));
+    void *ws = nullptr, *lz = nullptr;
+    PSDGB_TRY(resolve_ws(ds, n, precision, nullptr, 0, &ws));
+    PSDGB_TRY(resolve_lz(ds, n, 20, &lz));
+    // Earlier work on the caller's stream (e.g. writes of the host inputs'
+    // producers are the caller's business; device-side users of the staging
+    // buffers are only these calls) finishes before the first copy.
+    PSDGB_CUDA_TRY(cudaEventRecord(ds->comp_done[0], s));
+    PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_in, ds->comp_done[0], 0));
+    for (int64_t i = 0; i < count; ++i) {
+        const int b = static_cast<int>(i & 1);
+        double* d = reinterpret_cast<double*>(static_cast<char*>(ds->stage2) + b * stride);
+        if (i >= 2) PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_in, ds->out_done[b], 0));
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(d, h_in[i], bytes, cudaMemcpyHostToDevice, ds->copy_in));
+        PSDGB_CUDA_TRY(cudaEventRecord(ds->in_done[b], ds->copy_in));
+        PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->in_done[b], 0));
+        PSDGB_TRY(composite_enqueue(ds, precision, schedule, d, n, ws, true, 20, 1e-10, kDefaultSeed,
+                                    PSDGB_RESIDUAL_REFERENCE, lz, s, nullptr, nullptr, -1, 0));
+        PSDGB_CUDA_TRY(cudaEventRecord(ds->comp_done[b], s));
+        PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_out, ds->comp_done[b], 0));
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(h_out[i], d, bytes, cudaMemcpyDeviceToHost, ds->copy_out));
+        PSDGB_CUDA_TRY(cudaEventRecord(ds->out_done[b], ds->copy_out));
+    }
+    PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->out_done[(count - 1) & 1], 0));
+    return finish(ds, s);
+}
+
 uint64_t psdgb_kernel_launch_count(void) { return g_launches.load(); }
 
 int psdgb_set_product_config(int acc_mode) {

@@ -39,6 +39,12 @@ struct DeviceState {
     size_t lz_bytes = 0;
     int sm_count = 0;
     int cc_major = 0, cc_minor = 0;
+    // Host-sequence projections (psdgb_project_host_many): copy streams,
+    // ordering events and two staging matrices, created on first use.
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t in_done[2] = {nullptr, nullptr}, comp_done[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
+    void* stage2 = nullptr;
+    size_t stage2_bytes = 0;
 };
 psdgb_status device_state(DeviceState** out);
 // Synchronise the stream and turn a device error word into a status.

@@ -134,13 +134,14 @@ __global__ void lz_init_kernel(int64_t n, uint64_t seed, const double* __restric
 }
 
 // y[c] = sum_r A[c*ld + r] * x[r] for every column c of the symmetric FP32
-// matrix A (so y = A x = A^T x).  One warp per column, float4 loads, FP32
-// partial sums per lane flushed to FP64 every 64 vectors, FP64 across lanes.
+// matrix A (so y = A x = A^T x).  One or two adjacent columns per warp,
+// float4 loads, FP32 partial sums per lane flushed to FP64 every 64 vectors,
+// FP64 across lanes.
 // x is staged in shared memory.  Writes y as FP64 (y64) and/or FP32 (y32).
 // The whole kernel is skipped when *skip is non-zero.
 __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict__ A, int64_t n, int64_t ld,
                                                         const float* __restrict__ x, double* __restrict__ y64,
-                                                        float* __restrict__ y32, const int* skip) {
+                                                        float* __restrict__ y32, const int* skip, int pair) {
     if (skip != nullptr && *skip) return;
     extern __shared__ float4 xs4[];
     float* xs = reinterpret_cast<float*>(xs4);
@@ -149,31 +150,54 @@ __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict_
     __syncthreads();
     const int lane = threadIdx.x % 32;
     const int64_t warps_total = static_cast<int64_t>(gridDim.x) * (blockDim.x / 32);
-    for (int64_t c = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + threadIdx.x / 32; c < n;
-         c += warps_total) {
-        const float4* col = reinterpret_cast<const float4*>(A + c * ld);
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-        double acc = 0.0;
+    const int64_t units = pair ? (n + 1) / 2 : n;
+    // With `pair` each warp streams two adjacent columns with interleaved
+    // loads (twice the loads in flight per lane, for matrices with more
+    // columns than resident warps); a column's own arithmetic is the same
+    // either way.
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x / 32) + threadIdx.x / 32; u < units;
+         u += warps_total) {
+        const int64_t c0 = pair ? 2 * u : u;
+        const bool has1 = pair && c0 + 1 < n;
+        const float4* col0 = reinterpret_cast<const float4*>(A + c0 * ld);
+        const float4* col1 = has1 ? col0 + ld4 : col0;
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, t0 = 0.f, t1 = 0.f, t2 = 0.f, t3 = 0.f;
+        double acc0 = 0.0, acc1 = 0.0;
         int64_t k = lane;
         while (k < ld4) {
             const int64_t kend = (k + 32 * 64 < ld4) ? k + 32 * 64 : ld4;
 #pragma unroll 8
             for (; k < kend; k += 32) {
-                const float4 a = __ldg(col + k);
+                const float4 a = __ldg(col0 + k);
+                const float4 c = __ldg(col1 + k);
                 const float4 b = xs4[k];
                 s0 = fmaf(a.x, b.x, s0);
                 s1 = fmaf(a.y, b.y, s1);
                 s2 = fmaf(a.z, b.z, s2);
                 s3 = fmaf(a.w, b.w, s3);
+                t0 = fmaf(c.x, b.x, t0);
+                t1 = fmaf(c.y, b.y, t1);
+                t2 = fmaf(c.z, b.z, t2);
+                t3 = fmaf(c.w, b.w, t3);
             }
-            acc += static_cast<double>(s0) + static_cast<double>(s1) + static_cast<double>(s2) +
-                   static_cast<double>(s3);
+            acc0 += static_cast<double>(s0) + static_cast<double>(s1) + static_cast<double>(s2) +
+                    static_cast<double>(s3);
+            acc1 += static_cast<double>(t0) + static_cast<double>(t1) + static_cast<double>(t2) +
+                    static_cast<double>(t3);
             s0 = s1 = s2 = s3 = 0.f;
+            t0 = t1 = t2 = t3 = 0.f;
         }
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc0 += __shfl_xor_sync(0xffffffffu, acc0, o);
+            acc1 += __shfl_xor_sync(0xffffffffu, acc1, o);
+        }
         if (lane == 0) {
-            if (y64) y64[c] = acc;
-            if (y32) y32[c] = static_cast<float>(acc);
+            if (y64) y64[c0] = acc0;
+            if (y32) y32[c0] = static_cast<float>(acc0);
+            if (has1) {
+                if (y64) y64[c0 + 1] = acc1;
+                if (y32) y32[c0 + 1] = static_cast<float>(acc1);
+            }
         }
     }
 }
@@ -305,11 +329,22 @@ cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double
                    int sm_count, cudaStream_t s) {
     const size_t smem = sizeof(float) * static_cast<size_t>(ld);
     const int threads = 256;
-    int64_t blocks = (n + 7) / 8;  // one column per warp
-    const int64_t cap = static_cast<int64_t>(sm_count) * 8;
+    // At most the CTAs that fit at once (the loop strides over the rest);
+    // two columns per warp when one per warp would not fit in one wave.
+    static size_t cached_smem = 0;
+    static int per_sm = 0;
+    if (smem != cached_smem || per_sm < 1) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lz_matvec_kernel, threads, smem) != cudaSuccess ||
+            per_sm < 1)
+            per_sm = 1;
+        cached_smem = smem;
+    }
+    const int64_t cap = static_cast<int64_t>(sm_count) * per_sm;
+    const int pair = (n + 7) / 8 > cap ? 1 : 0;
+    int64_t blocks = pair ? ((n + 1) / 2 + 7) / 8 : (n + 7) / 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    lz_matvec_kernel<<<static_cast<unsigned>(blocks), threads, smem, s>>>(A, n, ld, x, y64, y32, skip);
+    lz_matvec_kernel<<<static_cast<unsigned>(blocks), threads, smem, s>>>(A, n, ld, x, y64, y32, skip, pair);
     count_launch();
     return cudaGetLastError();
 }

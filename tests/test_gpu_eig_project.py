@@ -80,3 +80,45 @@ def test_kernel_launches_are_counted(psd):
     psd.composite_FP32_auto_scale(t)
     # prologue + 20 Lanczos steps x 3 + Ritz + 10 filter steps x 3 + final >= 90
     assert psd.kernel_launch_count() - before >= 90
+
+
+def test_project_host_many_matches_one_call_per_matrix():
+    """The pipelined host sequence (copies of neighbouring matrices
+    overlapping each projection, two staging buffers) returns, for every
+    matrix, exactly what one synchronous call returns: the same device path
+    runs on the same input.  Buffers rotate (a buffer reused three steps
+    later) and one result overwrites its own input."""
+    import torch
+
+    import psd_projection_gb300 as psd
+
+    n = 300
+    rng = np.random.default_rng(5)
+    mats = []
+    for _ in range(5):
+        g = rng.standard_normal((n, n))
+        mats.append(0.5 * (g + g.T))
+    ins = [torch.from_numpy(m).pin_memory() for m in mats]
+    outs = [torch.empty_like(ins[0]).pin_memory() for _ in range(3)]
+    plan_out = [outs[0], outs[1], outs[2], outs[0], ins[4]]
+    expect = [psd.project_host("composite_FP32", m)[0] for m in mats]
+    psd.project_host_many("composite_FP32", ins, plan_out)
+    got = [None] * 5
+    got[4] = ins[4].numpy().copy()
+    got[3] = outs[0].numpy().copy()
+    got[2] = outs[2].numpy().copy()
+    got[1] = outs[1].numpy().copy()
+    for i in (1, 2, 3, 4):
+        assert np.array_equal(got[i], expect[i]), i
+    proj, _ = rp.eig_psd(mats[3])
+    assert rp.rel_frobenius(got[3], proj) <= 1e-4
+
+
+def test_project_host_many_validates():
+    import psd_projection_gb300 as psd
+
+    a = np.zeros((4, 4))
+    with pytest.raises(ValueError):
+        psd.project_host_many("composite_FP32", [a], [])
+    with pytest.raises(psd.PsdgbError, match="Unknown method"):
+        psd.project_host_many("nope", [a], [np.zeros((4, 4))])
