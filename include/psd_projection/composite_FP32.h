@@ -25,4 +25,13 @@ void composite_FP32(cublasHandle_t cublasH, double* mat, const int mat_size, flo
 void composite_FP32_auto_scale(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat, const int mat_size,
                                float* workspace = nullptr);
 
+/// Deflated projection (include/psd_projection/composite_FP32.h:32-45, work
+/// in progress in the reference): the k largest-|lambda| eigenpairs
+/// (compute_eigenpairs with max_iter = n and ortho_tol) are subtracted, the
+/// rest is scaled by 1.1 * bound + 1e-5 and filtered, and the positive pairs
+/// are added back.
+void composite_FP32_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                       const int mat_size, const size_t k = 40, const double tol = 1e-10,
+                                       const double ortho_tol = 1e-3, const bool verbose = false);
+
 #endif  // PSD_PROJECTION_COMPOSITE_FP32_H

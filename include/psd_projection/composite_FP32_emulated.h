@@ -19,6 +19,14 @@ void composite_FP32_emulated(cublasHandle_t cublasH, double* mat, const int mat_
 void composite_FP32_emulated_auto_scale(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
                                         const int mat_size, float* workspace = nullptr);
 
+/// The deflated projection with BF16x9 products.  The reference defines and
+/// exports it (src/composite_FP32_emulated.cu:264-325) without declaring it in
+/// its header; the declaration here gives the same symbol.  No defaults, as
+/// there is no reference declaration to take them from.
+void composite_FP32_emulated_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                                const int n, const size_t k, const double tol, const double ortho_tol,
+                                                const bool verbose);
+
 #endif  // CUDA_VERSION >= 12090
 
 #endif  // PSD_PROJECTION_COMPOSITE_FP32_EMULATED_H

@@ -260,6 +260,32 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
 
+/* ---- eigenpairs and deflation ------------------------------------------------- */
+/* Replaces compute_eigenpairs (include/psd_projection/lanczos.h:19-44,
+ * src/lanczos.cu:319-547): max_iter Lanczos steps on A (0 = n) with the basis
+ * kept, the Ritz pairs of T in order of decreasing |theta|, the residual
+ * filter |beta_m Z[0, j]| < ortho_tol (the reference compares with ortho_tol
+ * and ignores tol; its residual reads Z's first row) and the orthogonality
+ * filter |x_i . x_j| <= ortho_tol against the pairs already taken, up to k
+ * pairs.  Unless upper_bound_only, *r_out = r <= k, d_eigenvalues[0..r) and
+ * d_eigenvectors (n x r, column-major: vector i at offset i n) are written
+ * (k = 0 takes no pair).  *upper_out = |theta_max| + res + 1e-3, the
+ * reference's return value.  The start vector is the seeded SplitMix64
+ * stream of the Lanczos bound.  Allocates its basis (n (max_iter + 1)
+ * doubles) per call, as the reference does; synchronises `stream`. */
+psdgb_status psdgb_compute_eigenpairs(const double* d_A, int64_t n, int64_t k, int64_t* r_out, double* d_eigenvalues,
+                                      double* d_eigenvectors, int upper_bound_only, int64_t max_iter, double tol,
+                                      double ortho_tol, uint64_t seed, double* upper_out, void* stream);
+/* Replaces composite_FP32_auto_scale_deflate / composite_FP32_emulated_auto_scale_deflate
+ * (include/psd_projection/composite_FP32.h:32-45, src/composite_FP32.cu:193-254,
+ * src/composite_FP32_emulated.cu:264-325): the k largest-|lambda| Ritz pairs
+ * (psdgb_compute_eigenpairs, max_iter n) are subtracted, the rest is bounded
+ * (100 steps, upper_bound_only) and scaled by 1.1 up + 1e-5, filtered with
+ * `precision` / `schedule`, scaled back, and the positive pairs are added
+ * back.  The second eigenpair run uses seed + 1. */
+psdgb_status psdgb_composite_auto_scale_deflate(int precision, int schedule, double* d_mat, int64_t n, int64_t k,
+                                                double tol, double ortho_tol, uint64_t seed, void* stream);
+
 /* A sequence of `count` n x n host matrices (h_in[i] -> h_out[i]; a buffer
  * may appear more than once and h_out[i] may equal h_in[i], but h_out[i] must
  * not be h_in[i + 1], which is read while matrix i is projected) with one

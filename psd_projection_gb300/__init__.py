@@ -303,3 +303,46 @@ def set_product_tuning(knob: int, value: int) -> int:
     """TUNE_TILE_GROUP (tile rows per group of the tile order, 0 = row by row) or TUNE_TILE_SHAPE
     (TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256); returns the previous value."""
     return int(_capi.lib().psdgb_set_product_tuning(int(knob), int(value)))
+
+
+def compute_eigenpairs(A, k: int, upper_bound_only: bool = False, max_iter: int = 0, tol: float = 1e-10,
+                       ortho_tol: float = 1e-5, seed: int = DEFAULT_SEED, stream=None) -> dict:
+    """compute_eigenpairs (include/psd_projection/lanczos.h:19-44) on a float64
+    CUDA matrix: {"upper": bound, "r": pairs kept (None when upper_bound_only),
+    "values": (r,) tensor, "vectors": (r, n) tensor, row i = eigenvector i}."""
+    torch = _torch()
+    n = _check_mat(A)
+    kk = max(int(k), 0)
+    vals = torch.empty(max(kk, 1), dtype=torch.float64, device=A.device)
+    vecs = torch.empty((max(kk, 1), max(n, 1)), dtype=torch.float64, device=A.device)
+    r = ctypes.c_int64(-1)
+    up = ctypes.c_double(0.0)
+    st = _capi.lib().psdgb_compute_eigenpairs(
+        ctypes.c_void_p(A.data_ptr()), n, kk, ctypes.byref(r),
+        None if upper_bound_only else ctypes.c_void_p(vals.data_ptr()),
+        None if upper_bound_only else ctypes.c_void_p(vecs.data_ptr()), 1 if upper_bound_only else 0,
+        int(max_iter), float(tol), float(ortho_tol), int(seed), ctypes.byref(up), _stream_ptr(stream))
+    _capi.check(st, "psdgb_compute_eigenpairs")
+    if upper_bound_only:
+        return {"upper": up.value, "r": None, "values": None, "vectors": None}
+    return {"upper": up.value, "r": r.value, "values": vals[: r.value], "vectors": vecs[: r.value]}
+
+
+def composite_auto_scale_deflate(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, k: int = 40,
+                                 tol: float = 1e-10, ortho_tol: float = 1e-3, seed: int = DEFAULT_SEED,
+                                 stream=None) -> None:
+    """composite_FP32_auto_scale_deflate (include/psd_projection/composite_FP32.h:32-45)
+    with any precision, in place on a float64 CUDA matrix."""
+    n = _check_mat(mat)
+    st = _capi.lib().psdgb_composite_auto_scale_deflate(int(precision), int(schedule), ctypes.c_void_p(mat.data_ptr()),
+                                                        n, int(k), float(tol), float(ortho_tol), int(seed),
+                                                        _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite_auto_scale_deflate")
+
+
+def composite_FP32_auto_scale_deflate(mat, k: int = 40, tol: float = 1e-10, ortho_tol: float = 1e-3) -> None:
+    composite_auto_scale_deflate(mat, PREC_FP16X3, SCHEDULE_FP32, k, tol, ortho_tol)
+
+
+def composite_FP32_emulated_auto_scale_deflate(mat, k: int = 40, tol: float = 1e-10, ortho_tol: float = 1e-3) -> None:
+    composite_auto_scale_deflate(mat, PREC_BF16X9, SCHEDULE_FP32, k, tol, ortho_tol)

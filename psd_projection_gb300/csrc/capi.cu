@@ -14,14 +14,12 @@
 
 namespace psdgb {
 
-size_t composite_ws_bytes(int64_t n, int precision);
 psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                            bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
                            void* lz_state, cudaStream_t s, double* up_out);
-psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
-                               bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
-                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out,
-                               int bulk_precision, int refine_steps);
+psdgb_status eigenpairs_run(DeviceState* ds, cublasHandle_t blas, cusolverDnHandle_t solver, const double* A,
+                            int64_t n, int64_t k, bool upper_only, int64_t max_iter, double ortho_tol, uint64_t seed,
+                            int64_t* r_out, double* d_vals, double* d_vecs, double* upper_out, cudaStream_t s);
 
 namespace {
 
@@ -592,6 +590,99 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
         PSDGB_CUDA_TRY(cudaEventRecord(ds->out_done[b], ds->copy_out));
     }
     PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->out_done[(count - 1) & 1], 0));
+    return finish(ds, s);
+}
+
+psdgb_status psdgb_compute_eigenpairs(const double* d_A, int64_t n, int64_t k, int64_t* r_out, double* d_eigenvalues,
+                                      double* d_eigenvectors, int upper_bound_only, int64_t max_iter, double tol,
+                                      double ortho_tol, uint64_t seed, double* upper_out, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    (void)tol;  // as in the reference, the residual filter compares with ortho_tol (src/lanczos.cu:454)
+    if (n <= 0 || d_A == nullptr || k < 0 || max_iter < 0) {
+        set_error("compute_eigenpairs: need n > 0, a matrix, k >= 0 and max_iter >= 0");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (!upper_bound_only && k > 0 && (d_eigenvalues == nullptr || d_eigenvectors == nullptr)) {
+        set_error("compute_eigenpairs: eigenvalue and eigenvector outputs are required unless upper_bound_only");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    Handles& h = handles_for_device(ds->device);
+    return eigenpairs_run(ds, h.blas, h.solver, d_A, n, k, upper_bound_only != 0, max_iter, ortho_tol, seed, r_out,
+                          d_eigenvalues, d_eigenvectors, upper_out, static_cast<cudaStream_t>(stream));
+}
+
+// src/composite_FP32.cu:193-254 (and the BF16x9 twin, src/composite_FP32_emulated.cu:264-325).
+psdgb_status psdgb_composite_auto_scale_deflate(int precision, int schedule, double* d_mat, int64_t n, int64_t k,
+                                                double tol, double ortho_tol, uint64_t seed, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi) || (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16)) {
+        set_error("composite_auto_scale_deflate: unknown precision or schedule");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
+        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n < 0 || k < 0 || (n > 0 && d_mat == nullptr)) {
+        set_error("composite_auto_scale_deflate: bad matrix or k");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PSDGB_OK;
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    Handles& h = handles_for_device(ds->device);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int64_t kk = k < n ? k : n;
+    double *vals = nullptr, *vecs = nullptr, *coef = nullptr;
+    struct Free {
+        double** p[3];
+        ~Free() {
+            for (double** q : p)
+                if (*q) cudaFree(*q);
+        }
+    } release{{&vals, &vecs, &coef}};
+    if (kk > 0 && (cudaMalloc(&vals, sizeof(double) * kk) != cudaSuccess ||
+                   cudaMalloc(&vecs, sizeof(double) * kk * n) != cudaSuccess ||
+                   cudaMalloc(&coef, sizeof(double) * kk) != cudaSuccess)) {
+        cudaGetLastError();
+        set_error("composite_auto_scale_deflate: device allocation failed");
+        return PSDGB_ERR_OUT_OF_MEMORY;
+    }
+    // Step 1: the k largest-|lambda| Ritz pairs that pass the reference's filters.
+    int64_t r = 0;
+    double up_unused = 0.0;
+    if (kk > 0)
+        PSDGB_TRY(eigenpairs_run(ds, h.blas, h.solver, d_mat, n, kk, false, 0, ortho_tol, seed, &r, vals, vecs,
+                                 &up_unused, s));
+    (void)tol;
+    std::vector<double> hv(static_cast<size_t>(r)), hc(static_cast<size_t>(r));
+    if (r > 0) PSDGB_CUDA_TRY(cudaMemcpy(hv.data(), vals, sizeof(double) * r, cudaMemcpyDeviceToHost));
+    // Step 2: X -= sum_i lambda_i v_i v_i^T.
+    for (int64_t i = 0; i < r; ++i) hc[i] = -hv[i];
+    if (r > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, hc.data(), sizeof(double) * r, cudaMemcpyHostToDevice, s));
+        PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, vecs, coef, static_cast<int>(r), s));
+    }
+    // Step 3: bound of the deflated matrix (100 Lanczos steps), scale 1.1 up + 1e-5.
+    double up = 0.0;
+    PSDGB_TRY(eigenpairs_run(ds, h.blas, h.solver, d_mat, n, 0, true, 100, 1e-5, seed + 1, nullptr, nullptr, nullptr,
+                             &up, s));
+    const double scale = up > 0.0 ? 1.1 * up + 1e-5 : 1.0;
+    // Step 4: the filter of X / scale, scaled back.
+    void* ws = nullptr;
+    PSDGB_TRY(resolve_ws(ds, n, precision, nullptr, 0, &ws));
+    PSDGB_TRY(composite_enqueue_scaled(ds, precision, schedule, d_mat, n, ws, scale, s));
+    // Step 5: add the positive deflated pairs back.
+    for (int64_t i = 0; i < r; ++i) hc[i] = hv[i] > 0.0 ? hv[i] : 0.0;
+    if (r > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, hc.data(), sizeof(double) * r, cudaMemcpyHostToDevice, s));
+        PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, vecs, coef, static_cast<int>(r), s));
+    }
     return finish(ds, s);
 }
 

@@ -169,13 +169,13 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
 }
 
 // mat (in place) = (X + up * (Xs*A + A*Xs)/2) / 2, Xs = X / up, X read from
-// mat; up is read from the device (up_dev) when given, else 1.
+// mat; up is up_host times the device value up_dev when given.
 psdgb_status run_final(DeviceState* ds, int precision, const Layout& L, double* mat, int64_t n, const double* up_dev,
-                       const double* inv_up_dev, cudaStream_t s) {
-    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0, inv_up_dev, L.A2, L.fmt, L.np, s));
+                       const double* inv_up_dev, cudaStream_t s, double up_host = 1.0) {
+    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0 / up_host, inv_up_dev, L.A2, L.fmt, L.np, s));
     EpiParams ef = epi_base(L, n);
     ef.kind = EPI_FINAL;
-    ef.up = 1.0;
+    ef.up = up_host;
     ef.up_dev = up_dev;
     // (Xs*A + A*Xs)/2: the symmetric part of the product, as the reference's
     // symmetrisation of W does (src/composite_FP32.cu:153).
@@ -277,6 +277,26 @@ psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, dou
     PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s, bulk_precision, refine_steps));
     PSDGB_TRY(run_final(ds, precision, L, mat, n, up_dev, inv_up_dev, s));
     return PSDGB_OK;
+}
+
+// The filter of a matrix scaled by 1 / scale (a host value), and its result
+// scaled back: the reference's Dscal(1/scale), composite, Dscal(scale)
+// (src/composite_FP32.cu:233-243), with both scalings folded into the first
+// operand split and the final epilogue.
+psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                                      double scale, cudaStream_t s) {
+    PSDGB_TRY(check_n(n));
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi)) {
+        set_error("unknown precision");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PSDGB_OK;
+    if (!(scale > 0.0)) scale = 1.0;
+    const Layout L = make_layout(ws, pi.fmt, n);
+    PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0 / scale, nullptr, L.A, L.fmt, L.np, s));
+    PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s, -1, 0));
+    return run_final(ds, precision, L, mat, n, nullptr, nullptr, s, scale);
 }
 
 psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,

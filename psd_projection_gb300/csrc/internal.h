@@ -142,4 +142,16 @@ const double* lanczos_inv_scale_ptr(void* d_state, int64_t n, int64_t max_iter);
 psdgb_status lanczos_read(void* d_state, int64_t n, int64_t max_iter, cudaStream_t s, LanczosResult* res,
                           double* h_alpha, double* h_beta);
 
+// ---- shared by the entry points (capi.cu, composite.cu, eigenpairs.cu) --------
+size_t composite_ws_bytes(int64_t n, int precision);
+psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                               bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
+                               void* lz_state, cudaStream_t s, const double* d_warm, double* d_ritz_out,
+                               int bulk_precision, int refine_steps);
+psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
+                                      double scale, cudaStream_t s);
+
+// ---- eigenpairs and deflation (eigenpairs.cu) -----------------------------------
+// X += sum_i coef_i v_i v_i^T (column-major n x n; V n x r column-major; coef on the device).
+cudaError_t launch_rank_update(double* X, int64_t n, const double* V, const double* d_coef, int r, cudaStream_t s);
 }  // namespace psdgb

@@ -113,6 +113,50 @@ void approximate_two_norm(cublasHandle_t cublasH, cusolverDnHandle_t cusolverH, 
            "approximate_two_norm");
 }
 
+double compute_eigenpairs(cublasHandle_t cublasH, cusolverDnHandle_t cusolverH, const double* A, size_t n,
+                          const size_t k, size_t* r, double* eigenvalues, double* eigenvectors,
+                          const bool upper_bound_only, const size_t max_iter, const double tol, const double ortho_tol,
+                          const bool verbose) {
+    (void)cusolverH;
+    int64_t rr = 0;
+    double up = 0.0;
+    report(psdgb_compute_eigenpairs(A, static_cast<int64_t>(n), static_cast<int64_t>(k), &rr, eigenvalues,
+                                    eigenvectors, upper_bound_only ? 1 : 0, static_cast<int64_t>(max_iter), tol,
+                                    ortho_tol, kSeed, &up, stream_of(cublasH)),
+           "compute_eigenpairs");
+    if (!upper_bound_only) {
+        if (r) *r = static_cast<size_t>(rr);
+        if (verbose && static_cast<size_t>(rr) < k)
+            std::fprintf(stderr, "Warning: only %zu eigenpairs found, requested %zu.\n", static_cast<size_t>(rr), k);
+    }
+    return up;
+}
+
+namespace {
+void deflate_any(int precision, cublasHandle_t h, double* mat, int n, size_t k, double tol, double ortho_tol,
+                 const char* fn) {
+    report(psdgb_composite_auto_scale_deflate(precision, PSDGB_SCHEDULE_FP32, mat, n, static_cast<int64_t>(k), tol,
+                                              ortho_tol, kSeed, stream_of(h)),
+           fn);
+}
+}  // namespace
+
+void composite_FP32_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                       const int mat_size, const size_t k, const double tol, const double ortho_tol,
+                                       const bool verbose) {
+    (void)solverH;
+    (void)verbose;
+    deflate_any(PSDGB_PREC_FP16X3, cublasH, mat, mat_size, k, tol, ortho_tol, "composite_FP32_auto_scale_deflate");
+}
+
+void composite_FP32_emulated_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                                const int n, const size_t k, const double tol, const double ortho_tol,
+                                                const bool verbose) {
+    (void)solverH;
+    (void)verbose;
+    deflate_any(PSDGB_PREC_BF16X9, cublasH, mat, n, k, tol, ortho_tol, "composite_FP32_emulated_auto_scale_deflate");
+}
+
 double* eig_FP64_psd(cusolverDnHandle_t solverH, cublasHandle_t cublasH, double* mat, size_t mat_size,
                      bool return_eigenvalues) {
     (void)solverH;

@@ -131,3 +131,41 @@ def test_sym_upper_convention():
     x = np.arange(9.0).reshape(3, 3)
     s = rp.sym_upper(x)
     assert np.array_equal(s, s.T) and s[2, 0] == x[0, 2] and s[0, 2] == x[0, 2]
+
+
+# ---- eigenpairs and deflation (oracle/deflation_port.py) ----------------------
+
+KAT5 = np.array([[4, 1, 2, 0, 0], [1, 3, 0, 1, 0], [2, 0, 5, 1, 1], [0, 1, 1, 2, 1], [0, 0, 1, 1, 3]], dtype=float)
+
+
+def test_eigenpairs_port_kat():
+    """Lanczos.Eigenpairs (test/lanczos_test.hpp:44-84): the bound is at least
+    the quoted two-norm 7.0890; the three pairs kept are the top eigenpairs."""
+    from oracle import deflation_port as dp
+
+    ep = dp.compute_eigenpairs(KAT5, 3)
+    assert ep["upper"] >= 7.0890
+    w, V = np.linalg.eigh(KAT5)
+    order = np.argsort(-np.abs(w))[:3]
+    assert ep["r"] == 3
+    assert np.allclose(ep["values"], w[order], atol=1e-12)
+    assert np.allclose(np.abs(np.sum(ep["vectors"] * V[:, order], axis=0)), 1.0, atol=1e-10)
+    assert dp.compute_eigenpairs(KAT5, 0)["r"] == 0
+
+
+def test_deflate_port_kats():
+    """CompositeFP32.Simple5Deflate (test/composite_FP32_test.hpp:248-290; its
+    positional arguments give k = 0) within 1e-3 of diag(max(d, 0)), also
+    with k = 2; UniformAutoScaleDeflate1024's bar (Frobenius <= 0.1, k = 0) on
+    a smaller case of the same construction."""
+    from oracle import deflation_port as dp
+
+    d = np.diag([1.0, -2.0, 3.0, -4.0, 5.0])
+    for k in (0, 2):
+        out = dp.composite_auto_scale_deflate(d, "fp32", k=k, tol=2.0 if k == 0 else 1e-10)
+        assert np.abs(out - np.maximum(d, 0)).max() <= 1e-3
+    x = uniform_spectrum(256, 10.0, seed=4)
+    proj, _ = rp.eig_psd(x)
+    out = dp.composite_auto_scale_deflate(x, "fp32", k=0, tol=40, ortho_tol=1e-10)
+    assert np.linalg.norm(out - proj) <= 0.1
+    assert rp.rel_frobenius(out, proj) <= 1e-4
