@@ -22,4 +22,14 @@ void composite_FP16(cublasHandle_t cublasH, double* mat, const int n, float* flo
 void composite_FP16_auto_scale(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat, const int mat_size,
                                float* float_workspace = nullptr, __half* half_workspace = nullptr);
 
+/// Deflated FP16 projection (include/psd_projection/composite_FP16.h:35-50,
+/// work in progress in the reference): the k largest and k smallest
+/// eigenpairs (LOBPCG, maxiter, tol) are subtracted, the rest is bounded,
+/// scaled by 1.1 * bound + 1e-5 and filtered, and the positive pairs are
+/// added back.  Needs 3 k <= mat_size.  The workspaces are not needed.
+void composite_FP16_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                       const int mat_size, float* float_workspace = nullptr,
+                                       __half* half_workspace = nullptr, const size_t k = 40, const int maxiter = 100,
+                                       const double tol = 1e-10, const bool verbose = false);
+
 #endif  // PSD_PROJECTION_COMPOSITE_FP16_H

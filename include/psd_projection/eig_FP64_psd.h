@@ -15,4 +15,12 @@
 double* eig_FP64_psd(cusolverDnHandle_t solverH, cublasHandle_t cublasH, double* mat, size_t mat_size,
                      bool return_eigenvalues = false);
 
+/// Deflated EVD projection (include/psd_projection/eig_FP64_psd.h:22-31):
+/// the k largest and k smallest eigenpairs (LOBPCG) are subtracted, the rest
+/// is projected with Dsyevd, and the positive pairs are added back.  Needs
+/// 3 k <= mat_size.
+void eig_FP64_deflate(cusolverDnHandle_t solverH, cublasHandle_t cublasH, double* mat, size_t mat_size,
+                      const size_t k = 40, const int maxiter = 100, const double tol = 1e-10,
+                      const bool verbose = false);
+
 #endif  // PSD_PROJECTION_EIG_FP64_PSD_H

@@ -286,6 +286,29 @@ psdgb_status psdgb_compute_eigenpairs(const double* d_A, int64_t n, int64_t k, i
 psdgb_status psdgb_composite_auto_scale_deflate(int precision, int schedule, double* d_mat, int64_t n, int64_t k,
                                                 double tol, double ortho_tol, uint64_t seed, void* stream);
 
+/* Replaces lobpcg (include/psd_projection/lobpcg.h, src/lobpcg.cu:12-255):
+ * the m largest eigenpairs of the symmetric n x n device matrix A (0 < 3 m <= n)
+ * into d_V (n x m, column-major) and d_D (m values, decreasing).  warmstart
+ * takes d_V as the (orthonormal) start block, else the seeded stream is
+ * orthonormalised; stops when ||A X - X Lambda||_F < tol or after maxiter
+ * iterations (*iterations_out).  Synchronises `stream` once per iteration. */
+psdgb_status psdgb_lobpcg(const double* d_A, double* d_V, double* d_D, int64_t n, int64_t m, int warmstart,
+                          int maxiter, double tol, uint64_t seed, int* iterations_out, void* stream);
+/* Replaces eig_FP64_deflate (include/psd_projection/eig_FP64_psd.h:22-31,
+ * src/eig_FP64_psd.cu:87-177): the k largest and the k smallest eigenpairs
+ * (LOBPCG on X and on -X, maxiter, tol) are subtracted, the rest is projected
+ * by the FP64 EVD, and the positive parts are added back.  0 < 3 k <= n. */
+psdgb_status psdgb_eig_FP64_deflate(double* d_mat, int64_t n, int64_t k, int maxiter, double tol, uint64_t seed,
+                                    void* stream);
+/* Replaces composite_FP16_auto_scale_deflate (include/psd_projection/composite_FP16.h:35-50,
+ * src/composite_FP16.cu:276-380) for any precision / schedule: the same
+ * two-ended deflation, then the Lanczos bound (20 steps), scaling by
+ * 1.1 up + 1e-5, the composite filter, scaling back, and the positive parts
+ * added back.  0 < 3 k <= n. */
+psdgb_status psdgb_composite_auto_scale_deflate_two_ends(int precision, int schedule, double* d_mat, int64_t n,
+                                                         int64_t k, int maxiter, double tol, uint64_t seed,
+                                                         void* stream);
+
 /* A sequence of `count` n x n host matrices (h_in[i] -> h_out[i]; a buffer
  * may appear more than once and h_out[i] may equal h_in[i], but h_out[i] must
  * not be h_in[i + 1], which is read while matrix i is projected) with one

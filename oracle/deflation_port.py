@@ -127,3 +127,88 @@ def composite_auto_scale_deflate(X: np.ndarray, method: str = "fp32", k: int = 4
     fn = rp.composite_fp16 if method == "fp16" else rp.composite_fp32
     P = fn(Xd * (1.0 / scale)) * scale                        # :236-243
     return rank_update(P, np.maximum(vals, 0.0), V)           # :245-252
+
+
+def random_block(n: int, m: int, seed: int) -> np.ndarray:
+    """n x m block, column-major fill of the seeded uniform stream (the
+    reference fills with curand from seed 0, src/lobpcg.cu:93)."""
+    return rp.start_vector(n * m, seed).reshape(m, n).T.copy()
+
+
+def lobpcg(A: np.ndarray, m: int, warmstart_V=None, warmstart_D=None, maxiter: int = 100, tol: float = 1e-8,
+           seed: int = 0) -> dict:
+    """src/lobpcg.cu:12-255: block Rayleigh-Ritz on span[X, R, Delta] (QR of
+    the n x 3m block), the m largest Ritz pairs kept.  The first Rayleigh-Ritz
+    keeps its eigenvectors in ascending order while the values are reversed
+    (:121-127), as the reference does; the product X = Q T is formed out of
+    place (the reference's cublasDgemm writes over its own input, :125-127).
+    Returns {V (n x m), D (m,), iters}."""
+    import scipy.linalg
+
+    A = np.asarray(A, dtype=np.float64)
+    n = A.shape[0]
+    assert 0 < m and 3 * m <= n
+    if warmstart_V is not None:
+        X, lam = np.array(warmstart_V, dtype=np.float64), np.array(warmstart_D, dtype=np.float64)
+    else:
+        X, _ = np.linalg.qr(random_block(n, m, seed))                 # :89-100
+    T = X.T @ A @ X                                                   # :104-111
+    T = 0.5 * (T + T.T)                                               # :115-119
+    lt, Z = scipy.linalg.eigh(T, driver="evd")                        # :123-124
+    lam = lt[::-1].copy()                                             # :126
+    X = X @ Z                                                         # :129-131 (ascending order)
+    D = X.copy()                                                      # :134
+    iters = 0
+    for it in range(1, maxiter + 1):
+        R = A @ X - X * lam                                           # :138-152
+        iters = it
+        if np.linalg.norm(R) < tol:                                   # :154-163
+            break
+        Q, _ = np.linalg.qr(np.hstack([X, R, D]))                     # :166-172
+        T = Q.T @ A @ Q                                               # :174-182
+        T = 0.5 * (T + T.T)                                           # :186-190
+        la, Z = scipy.linalg.eigh(T, driver="evd")                    # :194-195
+        Z = Z[:, ::-1]                                                # :197
+        Xn = Q @ Z[:, :m]                                             # :200-202, :209-211
+        D = Xn - X                                                    # :205-214
+        X = Xn
+        lam = la[::-1][:m].copy()                                     # :217-218
+    return {"V": X, "D": lam, "iters": iters}
+
+
+def _deflate_both_ends(X: np.ndarray, k: int, maxiter: int, tol: float, seed: int):
+    """The two LOBPCG runs and subtractions of src/eig_FP64_psd.cu:104-150."""
+    top = lobpcg(X, k, maxiter=maxiter, tol=tol, seed=seed)
+    X = rank_update(X, -top["D"], top["V"])                            # :113-122
+    bot = lobpcg(-X, k, maxiter=maxiter, tol=tol, seed=seed)          # :125-131
+    X = rank_update(X, bot["D"], bot["V"])                            # :135-145 (values of -X)
+    return X, top, bot
+
+
+def _add_back(X: np.ndarray, top: dict, bot: dict) -> np.ndarray:
+    """src/eig_FP64_psd.cu:154-170: the positive parts of both deflated ends."""
+    X = rank_update(X, np.maximum(top["D"], 0.0), top["V"])
+    return rank_update(X, np.maximum(-bot["D"], 0.0), bot["V"])
+
+
+def eig_deflate(X: np.ndarray, k: int = 40, maxiter: int = 100, tol: float = 1e-10, seed: int = 0) -> np.ndarray:
+    """src/eig_FP64_psd.cu:87-177: deflate the k largest and k smallest
+    eigenpairs (LOBPCG), EVD-project the rest, add back the positive pairs."""
+    X = rp.sym_upper(np.asarray(X, dtype=np.float64))
+    Xd, top, bot = _deflate_both_ends(X, k, maxiter, tol, seed)
+    P, _ = rp.eig_psd(Xd)                                             # :150
+    return _add_back(P, top, bot)
+
+
+def composite_fp16_auto_scale_deflate(X: np.ndarray, k: int = 40, maxiter: int = 100, tol: float = 1e-10,
+                                      seed: int = 0, method: str = "fp16") -> np.ndarray:
+    """src/composite_FP16.cu:276-380: the same two-ended deflation, then the
+    Lanczos bound (20 steps), scaling by 1.1 up + 1e-5, the FP16 composite
+    filter, scaling back, and the positive pairs added back."""
+    X = rp.sym_upper(np.asarray(X, dtype=np.float64))
+    Xd, top, bot = _deflate_both_ends(X, k, maxiter, tol, seed)
+    up = rp.approximate_two_norm(Xd)["up"]                           # :343-346
+    scale = 1.1 * up + 1e-5 if up > 0.0 else 1.0                      # :349
+    fn = rp.composite_fp16 if method == "fp16" else rp.composite_fp32
+    P = fn(Xd * (1.0 / scale)) * scale                                # :351-358
+    return _add_back(P, top, bot)

@@ -1,6 +1,6 @@
 """Replay of the reference's GPU call sequence on cuBLAS through torch.
 
-TEST / BASELINE INFRASTRUCTURE ONLY (bench.py --impl reference).  The
+TEST / BENCHMARK INFRASTRUCTURE ONLY (bench.py --impl reference).  The
 reference library is a CUDA/cuBLAS library whose build needs its own x86
 objects; this port issues the same sequence of library calls so its speed
 can be measured on the GPU host:

@@ -346,3 +346,41 @@ def composite_FP32_auto_scale_deflate(mat, k: int = 40, tol: float = 1e-10, orth
 
 def composite_FP32_emulated_auto_scale_deflate(mat, k: int = 40, tol: float = 1e-10, ortho_tol: float = 1e-3) -> None:
     composite_auto_scale_deflate(mat, PREC_BF16X9, SCHEDULE_FP32, k, tol, ortho_tol)
+
+
+def lobpcg(A, m: int, V0=None, maxiter: int = 100, tol: float = 1e-8, seed: int = 0, stream=None) -> dict:
+    """lobpcg (include/psd_projection/lobpcg.h) on a float64 CUDA matrix: the
+    m largest eigenpairs.  V0 (m, n), rows orthonormal, warm-starts.  Returns
+    {"V": (m, n) tensor, row i = eigenvector i, "D": (m,) decreasing, "iters"}."""
+    torch = _torch()
+    n = _check_mat(A)
+    V = torch.empty((max(int(m), 1), n), dtype=torch.float64, device=A.device)
+    D = torch.empty(max(int(m), 1), dtype=torch.float64, device=A.device)
+    if V0 is not None:
+        V.copy_(V0)
+    iters = ctypes.c_int(0)
+    st = _capi.lib().psdgb_lobpcg(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(V.data_ptr()),
+                                  ctypes.c_void_p(D.data_ptr()), n, int(m), 1 if V0 is not None else 0, int(maxiter),
+                                  float(tol), int(seed), ctypes.byref(iters), _stream_ptr(stream))
+    _capi.check(st, "psdgb_lobpcg")
+    return {"V": V[: int(m)], "D": D[: int(m)], "iters": iters.value}
+
+
+def eig_FP64_deflate(mat, k: int = 40, maxiter: int = 100, tol: float = 1e-10, seed: int = 0, stream=None) -> None:
+    """eig_FP64_deflate (include/psd_projection/eig_FP64_psd.h:22-31), in place."""
+    n = _check_mat(mat)
+    st = _capi.lib().psdgb_eig_FP64_deflate(ctypes.c_void_p(mat.data_ptr()), n, int(k), int(maxiter), float(tol),
+                                            int(seed), _stream_ptr(stream))
+    _capi.check(st, "psdgb_eig_FP64_deflate")
+
+
+def composite_FP16_auto_scale_deflate(mat, k: int = 40, maxiter: int = 100, tol: float = 1e-10, seed: int = 0,
+                                      precision: int = PREC_FP16, schedule: int = SCHEDULE_FP16, stream=None) -> None:
+    """composite_FP16_auto_scale_deflate (include/psd_projection/composite_FP16.h:35-50), in place;
+    precision / schedule select the filter (the reference's is FP16)."""
+    n = _check_mat(mat)
+    st = _capi.lib().psdgb_composite_auto_scale_deflate_two_ends(int(precision), int(schedule),
+                                                                 ctypes.c_void_p(mat.data_ptr()), n, int(k),
+                                                                 int(maxiter), float(tol), int(seed),
+                                                                 _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite_auto_scale_deflate_two_ends")

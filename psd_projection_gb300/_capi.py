@@ -97,6 +97,10 @@ SIGNATURES = {
     "psdgb_compute_eigenpairs": (c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_int, c_i64, c_dbl, c_dbl, c_u64,
                                          c_vp, c_vp]),
     "psdgb_composite_auto_scale_deflate": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_dbl, c_u64, c_vp]),
+    "psdgb_lobpcg": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_int, c_int, c_dbl, c_u64, c_vp, c_vp]),
+    "psdgb_eig_FP64_deflate": (c_int, [c_vp, c_i64, c_i64, c_int, c_dbl, c_u64, c_vp]),
+    "psdgb_composite_auto_scale_deflate_two_ends": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_int, c_dbl, c_u64,
+                                                            c_vp]),
     "psdgb_kernel_launch_count": (c_u64, []),
     "psdgb_rel_frobenius": (c_int, [c_vp, c_vp, c_i64, P_dbl, c_vp]),
     "psdgb_filter_coefficients": (c_int, [c_int, ctypes.POINTER(ctypes.c_float), c_int]),

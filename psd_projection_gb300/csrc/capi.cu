@@ -20,6 +20,9 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
 psdgb_status eigenpairs_run(DeviceState* ds, cublasHandle_t blas, cusolverDnHandle_t solver, const double* A,
                             int64_t n, int64_t k, bool upper_only, int64_t max_iter, double ortho_tol, uint64_t seed,
                             int64_t* r_out, double* d_vals, double* d_vecs, double* upper_out, cudaStream_t s);
+psdgb_status lobpcg_run(DeviceState* ds, cublasHandle_t blas, cusolverDnHandle_t solver, const double* A, double* V,
+                        double* D, int64_t n, int64_t m, bool warmstart, int maxiter, double tol, uint64_t seed,
+                        int* iters_out, cudaStream_t s);
 
 namespace {
 
@@ -684,6 +687,118 @@ psdgb_status psdgb_composite_auto_scale_deflate(int precision, int schedule, dou
         PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, vecs, coef, static_cast<int>(r), s));
     }
     return finish(ds, s);
+}
+
+psdgb_status psdgb_lobpcg(const double* d_A, double* d_V, double* d_D, int64_t n, int64_t m, int warmstart,
+                          int maxiter, double tol, uint64_t seed, int* iterations_out, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (d_A == nullptr || d_V == nullptr || d_D == nullptr || maxiter < 0) {
+        set_error("lobpcg: null pointer or negative maxiter");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    Handles& h = handles_for_device(ds->device);
+    return lobpcg_run(ds, h.blas, h.solver, d_A, d_V, d_D, n, m, warmstart != 0, maxiter, tol, seed, iterations_out,
+                      static_cast<cudaStream_t>(stream));
+}
+
+namespace {
+
+// The two-ended deflation of src/eig_FP64_psd.cu:87-177 and
+// src/composite_FP16.cu:276-380: the k largest (LOBPCG on X) and k smallest
+// (LOBPCG on -X) eigenpairs are subtracted, the rest is projected (`eig`: the
+// FP64 EVD projection; else the Lanczos bound, scaling by 1.1 up + 1e-5 and
+// the composite filter), and the positive parts of both ends are added back.
+psdgb_status deflate_two_ends(bool eig, int precision, int schedule, double* d_mat, int64_t n, int64_t k, int maxiter,
+                              double tol, uint64_t seed, cudaStream_t s) {
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    if (!eig) PSDGB_TRY(require_sm103(ds));
+    Handles& h = handles_for_device(ds->device);
+    double *Vt = nullptr, *Dt = nullptr, *Vb = nullptr, *Db = nullptr, *coef = nullptr;
+    struct Free {
+        double** p[5];
+        ~Free() {
+            for (double** q : p)
+                if (*q) cudaFree(*q);
+        }
+    } release{{&Vt, &Dt, &Vb, &Db, &coef}};
+    if (cudaMalloc(&Vt, sizeof(double) * n * k) != cudaSuccess || cudaMalloc(&Vb, sizeof(double) * n * k) != cudaSuccess ||
+        cudaMalloc(&Dt, sizeof(double) * k) != cudaSuccess || cudaMalloc(&Db, sizeof(double) * k) != cudaSuccess ||
+        cudaMalloc(&coef, sizeof(double) * k) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("deflate: device allocation failed");
+        return PSDGB_ERR_OUT_OF_MEMORY;
+    }
+    const int kk = static_cast<int>(k);
+    const int64_t nn = n * n;
+    std::vector<double> top(k), bot(k), c(k);
+    // Largest: X -= lambda v v^T.
+    PSDGB_TRY(lobpcg_run(ds, h.blas, h.solver, d_mat, Vt, Dt, n, k, false, maxiter, tol, seed, nullptr, s));
+    PSDGB_CUDA_TRY(cudaMemcpy(top.data(), Dt, sizeof(double) * k, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < kk; ++i) c[i] = -top[i];
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, c.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, Vt, coef, kk, s));
+    // Smallest: LOBPCG on -X gives mu = -lambda; X += mu v v^T.
+    PSDGB_CUDA_TRY(launch_scale_inplace(d_mat, nn, -1.0, s));
+    PSDGB_TRY(lobpcg_run(ds, h.blas, h.solver, d_mat, Vb, Db, n, k, false, maxiter, tol, seed, nullptr, s));
+    PSDGB_CUDA_TRY(launch_scale_inplace(d_mat, nn, -1.0, s));
+    PSDGB_CUDA_TRY(cudaMemcpy(bot.data(), Db, sizeof(double) * k, cudaMemcpyDeviceToHost));
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, bot.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, Vb, coef, kk, s));
+    // The rest.
+    if (eig) {
+        PSDGB_TRY(do_eig(ds, 1, d_mat, n, nullptr, s));
+    } else {
+        double lo = 0.0, up = 0.0;
+        PSDGB_TRY(psdgb_two_norm(d_mat, n, &lo, &up, 20, 1e-10, seed, PSDGB_RESIDUAL_REFERENCE, nullptr, 0, s));
+        const double scale = up > 0.0 ? 1.1 * up + 1e-5 : 1.0;
+        void* ws = nullptr;
+        PSDGB_TRY(resolve_ws(ds, n, precision, nullptr, 0, &ws));
+        PSDGB_TRY(composite_enqueue_scaled(ds, precision, schedule, d_mat, n, ws, scale, s));
+    }
+    // Add back the positive parts: max(lambda_top, 0) and max(-mu_bottom, 0).
+    for (int i = 0; i < kk; ++i) c[i] = top[i] > 0.0 ? top[i] : 0.0;
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, c.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, Vt, coef, kk, s));
+    PSDGB_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int i = 0; i < kk; ++i) c[i] = -bot[i] > 0.0 ? -bot[i] : 0.0;
+    PSDGB_CUDA_TRY(cudaMemcpyAsync(coef, c.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    PSDGB_CUDA_TRY(launch_rank_update(d_mat, n, Vb, coef, kk, s));
+    return finish(ds, s);
+}
+
+psdgb_status check_deflate_args(double* d_mat, int64_t n, int64_t k, int maxiter) {
+    if (n < 0 || k <= 0 || 3 * k > n || maxiter < 0 || (n > 0 && d_mat == nullptr) || n > 2147483647LL) {
+        set_error("deflate: need a matrix, maxiter >= 0 and 0 < 3 k <= n (LOBPCG block, src/lobpcg.cu:25-27)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    return PSDGB_OK;
+}
+
+}  // namespace
+
+psdgb_status psdgb_eig_FP64_deflate(double* d_mat, int64_t n, int64_t k, int maxiter, double tol, uint64_t seed,
+                                    void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    PSDGB_TRY(check_deflate_args(d_mat, n, k, maxiter));
+    return deflate_two_ends(true, 0, 0, d_mat, n, k, maxiter, tol, seed, static_cast<cudaStream_t>(stream));
+}
+
+psdgb_status psdgb_composite_auto_scale_deflate_two_ends(int precision, int schedule, double* d_mat, int64_t n,
+                                                         int64_t k, int maxiter, double tol, uint64_t seed,
+                                                         void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi) || (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) ||
+        (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16)) {
+        set_error("composite deflate: unknown precision / schedule, or one-term BF16 without the FP16 schedule");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    PSDGB_TRY(check_deflate_args(d_mat, n, k, maxiter));
+    return deflate_two_ends(false, precision, schedule, d_mat, n, k, maxiter, tol, seed,
+                            static_cast<cudaStream_t>(stream));
 }
 
 uint64_t psdgb_kernel_launch_count(void) { return g_launches.load(); }

@@ -154,4 +154,6 @@ psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedu
 // ---- eigenpairs and deflation (eigenpairs.cu) -----------------------------------
 // X += sum_i coef_i v_i v_i^T (column-major n x n; V n x r column-major; coef on the device).
 cudaError_t launch_rank_update(double* X, int64_t n, const double* V, const double* d_coef, int r, cudaStream_t s);
+// x[i] *= a, i < count (lobpcg.cu).
+cudaError_t launch_scale_inplace(double* x, int64_t count, double a, cudaStream_t s);
 }  // namespace psdgb

@@ -24,6 +24,7 @@
 #include "psd_projection/eig_FP32_psd.h"
 #include "psd_projection/eig_FP64_psd.h"
 #include "psd_projection/lanczos.h"
+#include "psd_projection/lobpcg.h"
 #include "psdgb.h"
 
 namespace {
@@ -167,4 +168,33 @@ double* eig_FP32_psd(cusolverDnHandle_t solverH, cublasHandle_t cublasH, double*
                      bool return_eigenvalues) {
     (void)solverH;
     return eig_any(0, cublasH, mat, mat_size, return_eigenvalues, "eig_FP32_psd");
+}
+
+void lobpcg(cublasHandle_t cublasH, cusolverDnHandle_t cusolverH, const double* A, double* V, double* D, const int n,
+            const int m, const bool warmstart, const int maxiter, const double tol, const bool verbose) {
+    (void)cusolverH;
+    int iters = 0;
+    report(psdgb_lobpcg(A, V, D, n, m, warmstart ? 1 : 0, maxiter, tol, 0, &iters, stream_of(cublasH)), "lobpcg");
+    if (verbose) std::printf("LOBPCG: %d iterations\n", iters);
+}
+
+void eig_FP64_deflate(cusolverDnHandle_t solverH, cublasHandle_t cublasH, double* mat, size_t mat_size, const size_t k,
+                      const int maxiter, const double tol, const bool verbose) {
+    (void)solverH;
+    (void)verbose;
+    report(psdgb_eig_FP64_deflate(mat, static_cast<int64_t>(mat_size), static_cast<int64_t>(k), maxiter, tol, 0,
+                                  stream_of(cublasH)),
+           "eig_FP64_deflate");
+}
+
+void composite_FP16_auto_scale_deflate(cublasHandle_t cublasH, cusolverDnHandle_t solverH, double* mat,
+                                       const int mat_size, float* float_workspace, __half* half_workspace,
+                                       const size_t k, const int maxiter, const double tol, const bool verbose) {
+    (void)solverH;
+    (void)float_workspace;
+    (void)half_workspace;
+    (void)verbose;
+    report(psdgb_composite_auto_scale_deflate_two_ends(PSDGB_PREC_FP16, PSDGB_SCHEDULE_FP16, mat, mat_size,
+                                                       static_cast<int64_t>(k), maxiter, tol, 0, stream_of(cublasH)),
+           "composite_FP16_auto_scale_deflate");
 }

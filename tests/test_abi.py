@@ -65,6 +65,7 @@ def test_cpp_drop_in_compiles_and_links(lib, tmp_path):
 #include "psd_projection/eig_FP32_psd.h"
 #include "psd_projection/eig_FP64_psd.h"
 #include "psd_projection/lanczos.h"
+#include "psd_projection/lobpcg.h"
 int main(int argc, char**) {
     if (argc > 5) {  // never runs; only the link matters here
         cublasHandle_t h = nullptr; cusolverDnHandle_t s = nullptr; double* m = nullptr; double lo, up;
@@ -78,6 +79,9 @@ int main(int argc, char**) {
         compute_eigenpairs(h, s, m, 8, 0, nullptr, nullptr, nullptr, true, 100, 1e-10, 1e-5);
         composite_FP32_auto_scale_deflate(h, s, m, 8); composite_FP32_auto_scale_deflate(h, s, m, 8, 0, 2);
         composite_FP32_emulated_auto_scale_deflate(h, s, m, 8, 2, 1e-10, 1e-3, false);
+        lobpcg(h, s, m, m, m, 6, 2); lobpcg(h, s, m, m, m, 6, 2, 100, 1e-8, true);
+        eig_FP64_deflate(s, h, m, 8); eig_FP64_deflate(s, h, m, 8, 2, 50, 1e-8, false);
+        composite_FP16_auto_scale_deflate(h, s, m, 8); composite_FP16_auto_scale_deflate(h, s, m, 8, nullptr, nullptr, 2);
     }
     return 0;
 }

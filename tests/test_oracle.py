@@ -169,3 +169,37 @@ def test_deflate_port_kats():
     out = dp.composite_auto_scale_deflate(x, "fp32", k=0, tol=40, ortho_tol=1e-10)
     assert np.linalg.norm(out - proj) <= 0.1
     assert rp.rel_frobenius(out, proj) <= 1e-4
+
+
+A6 = np.array([[4, 1, 2, 0, 0, 0], [1, 3, 0, 1, 0, 0], [2, 0, 5, 1, 1, 0], [0, 1, 1, 2, 1, 1], [0, 0, 1, 1, 3, 2],
+               [0, 0, 0, 1, 2, 4]], dtype=float)
+
+
+def test_lobpcg_port_kats():
+    """LOBPCG.Simple (test/lobpcg_test.hpp:10-57: 7.3191, 5.6639 within 1e-4)
+    and LOBPCG.Random (:59-130: the m = n / 10 largest eigenvalues of R + R^T,
+    R ~ U[0, 1], within 1e-8 of EVD), at n = 100."""
+    from oracle import deflation_port as dp
+
+    r = dp.lobpcg(A6, 2)
+    assert np.allclose(r["D"], [7.3191, 5.6639], atol=1e-4)
+    rng = np.random.default_rng(0)
+    R = rng.random((100, 100))
+    A = R + R.T
+    r = dp.lobpcg(A, 10)
+    assert np.abs(r["D"] - np.linalg.eigvalsh(A)[::-1][:10]).max() <= 1e-8
+
+
+def test_two_ended_deflations_port():
+    """CompositeFP16.Random's bar (rel <= 1e-3 against EVD, n = 100, k = n / 10)
+    and the EVD deflation (exact up to LOBPCG's tolerance)."""
+    from oracle import deflation_port as dp
+
+    rng = np.random.default_rng(1)
+    R = rng.random((100, 100))
+    A = R + R.T
+    proj, _ = rp.eig_psd(A)
+    assert rp.rel_frobenius(dp.composite_fp16_auto_scale_deflate(A, k=10), proj) <= 1e-3
+    x = uniform_spectrum(120, 1.0, seed=2)
+    proj, _ = rp.eig_psd(x)
+    assert rp.rel_frobenius(dp.eig_deflate(x, k=10), proj) <= 1e-7
