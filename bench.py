@@ -406,6 +406,72 @@ def config3_session(n: int = 16384, seed: int = 3) -> dict:
 # block-diagonal batch: 4096 uneven blocks
 # ---------------------------------------------------------------------------
 
+def deflation_session(n: int = 1024, seed: int = 1) -> dict:
+    """The eigenpair / deflation routines (the reference's work-in-progress
+    family) at n = 1024 on the uniform spectrum lambda in [-10, 10] (the
+    reference tests' construction): GPU wall time of one call (after a warm
+    call), error against the host FP64 EVD projection, and the CPU
+    restatement's time on the same input where it finishes in seconds."""
+    import numpy as np
+    import torch
+
+    import psd_projection_gb300 as psd
+    from oracle import deflation_port as dp
+    from oracle import reference_port as rp
+
+    rng = np.random.default_rng(seed)
+    q, _ = np.linalg.qr(rng.random((n, n)) - 0.5)
+    x = (q * np.linspace(-10.0, 10.0, n)) @ q.T
+    proj, _ = rp.eig_psd(x)
+    d = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+    def gpu(fn, reps=3):
+        w = d.clone()
+        fn(w)
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            w = d.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            fn(w)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best * 1e3, w.cpu().numpy()
+
+    def cpu(fn):
+        t0 = time.perf_counter()
+        out = fn()
+        return time.perf_counter() - t0, out
+
+    res = {}
+    ms, out = gpu(lambda w: psd.composite_FP32_auto_scale_deflate(w, k=40, ortho_tol=1e-8))
+    cs, cout = cpu(lambda: dp.composite_auto_scale_deflate(x, "fp32", k=40, ortho_tol=1e-8))
+    res["composite_FP32_auto_scale_deflate_k40"] = {
+        "gpu_ms": ms, "rel_frobenius_err": rp.rel_frobenius(out, proj), "cpu_port_s": cs,
+        "cpu_port_err": rp.rel_frobenius(cout, proj), "note": "ortho_tol 1e-8; 1024 Lanczos steps"}
+    ms, out = gpu(lambda w: psd.eig_FP64_deflate(w, k=40))
+    res["eig_FP64_deflate_k40"] = {"gpu_ms": ms, "rel_frobenius_err": rp.rel_frobenius(out, proj)}
+    ms, out = gpu(lambda w: psd.composite_FP16_auto_scale_deflate(w, k=100))
+    res["composite_FP16_auto_scale_deflate_k100"] = {"gpu_ms": ms, "rel_frobenius_err": rp.rel_frobenius(out, proj)}
+    ms, _ = gpu(lambda w: psd.compute_eigenpairs(w, 40, ortho_tol=1e-8))
+    res["compute_eigenpairs_k40"] = {"gpu_ms": ms}
+    rr = np.random.default_rng(7).random((1000, 1000))
+    a = torch.from_numpy(rr + rr.T).cuda()
+    psd.lobpcg(a, 100)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lr = psd.lobpcg(a, 100)
+    torch.cuda.synchronize()
+    lms = (time.perf_counter() - t0) * 1e3
+    w = np.linalg.eigvalsh(rr + rr.T)[::-1][:100]
+    res["lobpcg_n1000_m100"] = {"gpu_ms": lms, "iters": lr["iters"],
+                                "max_eig_err": float(np.abs(lr["D"].cpu().numpy() - w).max())}
+    res["workload"] = (f"n={n}, A = Q diag(linspace(-10, 10)) Q^T, Q = QR(U[-0.5, 0.5]) seed {seed}; "
+                       "lobpcg on R + R^T, R ~ U[0, 1], n = 1000, m = 100 (the reference's LOBPCG.Random)")
+    return res
+
+
 def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_sample: int = 8) -> dict:
     """4096 blocks, n log-uniform in [16, 512] (seeded), entries (G + G^T)/2,
     stored FP32; the whole batch projected by one plan inside one captured CUDA
@@ -665,6 +731,7 @@ def run_ours(args, rank, world):
     if not args.no_configs:
         out["config1"] = config1_session()
         out["config3"] = config3_session()
+        out["deflation"] = deflation_session()
 
     if not args.no_serve:
         sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
@@ -745,7 +812,8 @@ def main():
         print(json.dumps({"batched": batched_session(count=args.batch_count)}))
         return
     if args.only_configs:
-        print(json.dumps({"config1": config1_session(), "config3": config3_session()}))
+        print(json.dumps({"config1": config1_session(), "config3": config3_session(),
+                          "deflation": deflation_session()}))
         return
     res = run_reference(args, rank, world) if args.impl == "reference" else run_ours(args, rank, world)
     if rank == 0 and res is not None:
