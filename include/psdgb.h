@@ -324,6 +324,14 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
                                      int64_t count, void* stream);
 
 /* ---- diagnostics ------------------------------------------------------------ */
+/* Exercises the device-side failure path: one GPU thread waits on an mbarrier
+ * that nothing arrives at, with the same bounded-wait code the product
+ * kernels use but a limit of limit_seconds (0.001 .. 5); the wait gives up,
+ * records a device error word and the kernel returns.  Expected result:
+ * PSDGB_ERR_DEVICE_TIMEOUT, with the error word cleared and the context
+ * usable afterwards.  No counterpart in the reference. */
+psdgb_status psdgb_selftest_wait_timeout(double limit_seconds, void* stream);
+
 /* Accumulator configuration of the tensor-core products of single-matrix
  * calls: -1 = automatic (default: four interleaved K accumulators for long
  * FP32-class products, double-buffered ones otherwise), 0 = four interleaved
@@ -350,8 +358,16 @@ int psdgb_set_product_config(int acc_mode);
  *   PSDGB_TUNE_WIDE_KBLOCK K block of a pipeline stage of the 128 x 256 tiles:
  *                          0 = by precision (default: 32 for two-term, 64 for
  *                          one-term products), 64 (128-byte rows) or 32
- *                          (64-byte rows, twice the stages). */
-enum { PSDGB_TUNE_TILE_GROUP = 1, PSDGB_TUNE_TILE_SHAPE = 2, PSDGB_TUNE_WIDE_KBLOCK = 3 };
+ *                          (64-byte rows, twice the stages);
+ *   PSDGB_TUNE_GROUP_EPI_WARPS  epilogue warps of the 128 x 128 kernel when it
+ *                          runs four accumulator buffers (short K: batches and
+ *                          small matrices): 4 or 8. */
+enum {
+    PSDGB_TUNE_TILE_GROUP = 1,
+    PSDGB_TUNE_TILE_SHAPE = 2,
+    PSDGB_TUNE_WIDE_KBLOCK = 3,
+    PSDGB_TUNE_GROUP_EPI_WARPS = 4
+};
 int psdgb_set_product_tuning(int knob, int value);
 
 /* Product-kernel timing: when enabled, the library records a CUDA event pair

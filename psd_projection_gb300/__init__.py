@@ -291,6 +291,7 @@ def rel_frobenius(a, b, stream=None) -> float:
 TUNE_TILE_GROUP = 1
 TUNE_TILE_SHAPE = 2
 TUNE_WIDE_KBLOCK = 3
+TUNE_GROUP_EPI_WARPS = 4
 TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256 = -1, 0, 1, 2
 
 

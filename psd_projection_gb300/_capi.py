@@ -26,6 +26,8 @@ STATUS_NAMES = {
     6: "PSDGB_ERR_SOLVER",
     7: "PSDGB_ERR_WORKSPACE_TOO_SMALL",
 }
+ERR_INVALID_ARGUMENT = 1
+ERR_DEVICE_TIMEOUT = 5
 
 # psdgb_precision
 PREC_FP32_SIMT = 0
@@ -97,6 +99,7 @@ SIGNATURES = {
     "psdgb_compute_eigenpairs": (c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_int, c_i64, c_dbl, c_dbl, c_u64,
                                          c_vp, c_vp]),
     "psdgb_composite_auto_scale_deflate": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_dbl, c_u64, c_vp]),
+    "psdgb_selftest_wait_timeout": (c_int, [c_dbl, c_vp]),
     "psdgb_lobpcg": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_int, c_int, c_dbl, c_u64, c_vp, c_vp]),
     "psdgb_eig_FP64_deflate": (c_int, [c_vp, c_i64, c_i64, c_int, c_dbl, c_u64, c_vp]),
     "psdgb_composite_auto_scale_deflate_two_ends": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_int, c_dbl, c_u64,

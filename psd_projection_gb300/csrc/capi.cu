@@ -421,6 +421,19 @@ psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_sched
     return finish(ds, s);
 }
 
+psdgb_status psdgb_selftest_wait_timeout(double limit_seconds, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (!(limit_seconds >= 0.001 && limit_seconds <= 5.0)) {
+        set_error("selftest: limit must be in [0.001, 5] seconds");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PSDGB_CUDA_TRY(launch_wait_selftest(ds->d_error, static_cast<uint64_t>(limit_seconds * 1e9), s));
+    return finish(ds, s);
+}
+
 psdgb_status psdgb_check_device_error(void) {
     DeviceState* ds = nullptr;
     PSDGB_TRY(device_state(&ds));
@@ -819,6 +832,11 @@ int psdgb_set_product_tuning(int knob, int value) {
         case PSDGB_TUNE_TILE_SHAPE: {
             const int prev = g_tile_shape;
             if (value >= -1 && value <= TILE_WIDE_128X256) g_tile_shape = value;
+            return prev;
+        }
+        case PSDGB_TUNE_GROUP_EPI_WARPS: {
+            const int prev = g_group_epi_warps;
+            if (value == 4 || value == 8) g_group_epi_warps = value;
             return prev;
         }
         case PSDGB_TUNE_WIDE_KBLOCK: {

@@ -134,7 +134,8 @@ enum DeviceError : int {
     DEVERR_TMA_WAIT = 1,     // producer gave up waiting for a free stage
     DEVERR_MMA_WAIT = 2,     // MMA warp gave up waiting for loaded operands
     DEVERR_EPI_WAIT = 3,     // epilogue gave up waiting for the accumulator
-    DEVERR_DRAIN_WAIT = 4    // in-flight copies/MMAs did not drain after an abort
+    DEVERR_DRAIN_WAIT = 4,   // in-flight copies/MMAs did not drain after an abort
+    DEVERR_SELFTEST_WAIT = 5 // the self-test's wait on a barrier nothing arrives at gave up (expected)
 };
 
 #if defined(__CUDACC__)
@@ -177,14 +178,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Wait for the phase with the given parity to complete; false after kWaitLimitNs.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Wait for the phase with the given parity to complete; false after limit_ns.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     while (!mbar_try_wait(bar, parity)) {
-        if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
     }
     return true;
+}
+// Wait for the phase with the given parity to complete; false after kWaitLimitNs.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    return mbar_wait_limit(bar, parity, kWaitLimitNs);
 }
 
 // ---- TMA ------------------------------------------------------------------

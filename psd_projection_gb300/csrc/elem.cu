@@ -197,4 +197,23 @@ cudaError_t launch_f32_to_f64(const float* in, double* out, int64_t count, cudaS
     return cudaGetLastError();
 }
 
+// Self-test of the bounded waits: one thread waits on an mbarrier that no
+// thread or copy ever arrives at; the wait gives up after limit_ns and records
+// DEVERR_SELFTEST_WAIT, and the kernel returns with nothing in flight.
+__global__ void wait_selftest_kernel(int* err, uint64_t limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait_limit(&bar, 0, limit_ns)) atomicCAS(err, 0, DEVERR_SELFTEST_WAIT);
+}
+
+cudaError_t launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t s) {
+    wait_selftest_kernel<<<1, 32, 0, s>>>(err, limit_ns);
+    count_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace psdgb

@@ -48,8 +48,8 @@ namespace {
 
 // ---- the kernel --------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS>
-__global__ void __launch_bounds__(THREADS, 1)
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW>
+__global__ void __launch_bounds__(64 + 32 * EW, 1)
     tc_group_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, const GroupWork gw, int num_tiles,
                     int* err) {
     using Cfg = TcCfg<TERMS>;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int b = 0; b < ACC_BUFS; ++b) {
             mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], EPI_WARPS);  // one arrival per epilogue warp
+            mbar_init(&acc_empty[b], EW);  // one arrival per epilogue warp
         }
         mbar_init(drain, 1);
         *abort_flag = 0;
@@ -185,8 +185,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             umma_commit(&acc_full[buf]);
         }
     } else if (warp >= 2) {
-        // ---- epilogue ----
+        // ---- epilogue: EW warps, EW / 4 per TMEM lane quarter, each on a
+        // slice of the tile's columns ----
         const int q4 = warp & 3;  // TMEM lane quarter this warp may access
+        constexpr int SLICE = BN / (EW / 4);
+        const int c_begin = ((warp - 2) / 4) * SLICE;
         int it = 0;
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
@@ -204,9 +207,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
             const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
             if (ep.fmt == FMT_F16)
-                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
+                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
             else
-                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
+                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -242,11 +245,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 // ---- host side -------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW>
 psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
     using Cfg = TcCfg<TERMS>;
-    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS>;
+    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW>;
     static bool configured = false;  // attribute set once per process (per instantiation)
     if (!configured) {
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
@@ -264,7 +267,7 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
     if (num_tiles <= 0) return PSDGB_OK;
     int g = grid > 0 ? grid : ds->sm_count;
     if (g > num_tiles) g = static_cast<int>(num_tiles);
-    kern<<<static_cast<unsigned>(g), THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, gw, static_cast<int>(num_tiles),
+    kern<<<static_cast<unsigned>(g), 64 + 32 * EW, Cfg::SMEM_BYTES, s>>>(tm, ep, gw, static_cast<int>(num_tiles),
                                                                     ds->d_error);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
@@ -276,9 +279,14 @@ psdgb_status launch_acc(DeviceState* ds, int acc_mode, const SplitMat& P, const 
                         int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid,
                         cudaStream_t s) {
     switch (acc_mode) {
-        case ACC_4X1: return launch_tc<TERMS, NPROD, BF16, 4, 1>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
-        case ACC_2X2: return launch_tc<TERMS, NPROD, BF16, 2, 2>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
-        case ACC_1X4: return launch_tc<TERMS, NPROD, BF16, 1, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_4X1: return launch_tc<TERMS, NPROD, BF16, 4, 1, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_2X2: return launch_tc<TERMS, NPROD, BF16, 2, 2, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_1X4:
+            // Short-K tiles (block-diagonal batches, small matrices) are
+            // epilogue-bound: twice the epilogue warps, each on half the columns.
+            if (g_group_epi_warps == 8)
+                return launch_tc<TERMS, NPROD, BF16, 1, 4, 8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+            return launch_tc<TERMS, NPROD, BF16, 1, 4, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         default: break;
     }
     set_error("gemm_tc: unknown accumulator mode");
@@ -353,6 +361,7 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
 
 int g_single_acc_mode = -1;
 int g_tile_group_rows = 8;
+int g_group_epi_warps = 8;
 
 // Accumulator configuration: the accuracy of one tensor-core FP32 accumulator
 // degrades with the number of K blocks it sums (n = 8192: 4.3e-5 rel. error

@@ -107,6 +107,7 @@ int auto_acc_mode(int precision, int64_t np);
 // chooses: 128 x 256 for one- and two-term precisions at np >= 2048.
 enum TileShape : int { TILE_128X128 = 0, TILE_PAIR_256X128 = 1, TILE_WIDE_128X256 = 2 };
 extern int g_tile_shape;
+extern int g_group_epi_warps;  // epilogue warps of 128 x 128 tiles with four accumulator buffers: 4 or 8
 extern int g_wide_kblock;  // K block of the 128 x 256 kernel: 64, 32, or 0 (by precision)
 extern int g_tile_group_rows;  // tile order of single-matrix products (grouped_decode), 0 = row by row
 // One matrix on CTA pairs (gemm_tc2.cu): 256 x 128 tiles, one
@@ -154,6 +155,8 @@ psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedu
 // ---- eigenpairs and deflation (eigenpairs.cu) -----------------------------------
 // X += sum_i coef_i v_i v_i^T (column-major n x n; V n x r column-major; coef on the device).
 cudaError_t launch_rank_update(double* X, int64_t n, const double* V, const double* d_coef, int r, cudaStream_t s);
+// One wait on a barrier nothing arrives at, bounded by limit_ns (elem.cu).
+cudaError_t launch_wait_selftest(int* err, uint64_t limit_ns, cudaStream_t s);
 // x[i] *= a, i < count (lobpcg.cu).
 cudaError_t launch_scale_inplace(double* x, int64_t count, double a, cudaStream_t s);
 }  // namespace psdgb

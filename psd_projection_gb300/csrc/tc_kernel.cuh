@@ -267,12 +267,13 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
 }
 
 // Epilogue of one tile for the warp whose first local row is p0 (lane = row
-// p0 + lane), reading the accumulators from TMEM.  TN is the tile width (the
-// MMA's N): ti.bj counts column tiles of TN, and the ACC_SPLIT accumulators
-// of a tile sit TN TMEM columns apart.
+// p0 + lane), reading the accumulators from TMEM, columns [c_begin, c_end)
+// of the tile.  TN is the tile width (the MMA's N): ti.bj counts column tiles
+// of TN, and the ACC_SPLIT accumulators of a tile sit TN TMEM columns apart.
 template <int FMT, int ACC_SPLIT, int TN = BN>
-__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc) {
-    for (int c0 = 0; c0 < TN; c0 += 32) {
+__device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc,
+                              int c_begin = 0, int c_end = TN) {
+    for (int c0 = c_begin; c0 < c_end; c0 += 32) {
         float v[32];
         tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
 #pragma unroll
