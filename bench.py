@@ -723,6 +723,23 @@ def run_ours(args, rank, world):
             side[name] = {"proj_s": 1e3 / ms, "ms": ms, "rel_frobenius_err": psd.rel_frobenius(inputs[steps], P),
                           "method": {"fp16": "composite_FP16", "bf16x9": "composite_FP32_emulated",
                                      "fp32_simt": "plain FP32 (CUDA cores)"}.get(name, name)}
+        # FP32 in / FP32 out (psdgb_composite_auto_scale_f32, asynchronous):
+        # the same projection for callers whose iterate is FP32.
+        x32 = [X.float() for _ in range(4)]
+        psd.composite_f32(x32[0])
+        torch.cuda.synchronize()
+        for t32 in x32[1:]:
+            t32.copy_(X)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for t32 in x32[1:]:
+            psd.composite_f32(t32)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 3
+        side["fp16x3_fp32_io"] = {"proj_s": 1e3 / ms, "ms": ms,
+                                  "rel_frobenius_err": psd.rel_frobenius(x32[-1].double(), P),
+                                  "method": "psdgb_composite_auto_scale_f32 (FP32 input and output)"}
         out["side_by_side"] = side
 
     if not args.no_batch:

@@ -149,6 +149,21 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
                                               void* d_ws, size_t ws_bytes, void* d_lanczos,
                                               size_t lanczos_bytes, void* stream);
 
+/* The auto-scaled projection of an FP32 matrix, in place, for callers whose
+ * iterate is FP32 (an ADMM loop): d_mat is n x n column-major FP32 on the
+ * device and its upper triangle defines it.  The Lanczos bound streams an
+ * FP32 copy as in the FP64 path, the filter runs at `precision` (a
+ * tensor-core precision), and the final reconstruction computes in FP64 and
+ * writes FP32: the FP64 path's result rounded to FP32, with half its HBM and
+ * host-copy traffic.  Warm start / Ritz output as in
+ * psdgb_composite_auto_scale_async.  Asynchronous: no host synchronisation;
+ * d_ws / d_lanczos may be null (the library's cached buffers are used, so the
+ * call must not race another call that uses them). */
+psdgb_status psdgb_composite_auto_scale_f32(int precision, int schedule, float* d_mat, int64_t n, int64_t max_iter,
+                                            double tol, uint64_t seed, int residual_mode, const double* d_warm_start,
+                                            double* d_ritz_out, void* d_ws, size_t ws_bytes, void* d_lanczos,
+                                            size_t lanczos_bytes, void* stream);
+
 /* Mixed precision (no counterpart in the reference): the Lanczos bound, the
  * bulk_schedule's steps with bulk_precision products (one-term FP16 or BF16),
  * then refine_steps steps of the quintic that ends the FP32 table (no safety

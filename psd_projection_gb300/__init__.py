@@ -385,3 +385,21 @@ def composite_FP16_auto_scale_deflate(mat, k: int = 40, maxiter: int = 100, tol:
                                                                  int(maxiter), float(tol), int(seed),
                                                                  _stream_ptr(stream))
     _capi.check(st, "psdgb_composite_auto_scale_deflate_two_ends")
+
+
+def composite_f32(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, max_iter: int = 20,
+                  tol: float = 1e-10, seed: int = DEFAULT_SEED, residual: int = RESIDUAL_REFERENCE, warm_start=None,
+                  ritz_out=None, stream=None) -> None:
+    """The auto-scaled projection of a float32 CUDA matrix, in place, asynchronous
+    (psdgb_composite_auto_scale_f32); warm_start / ritz_out are float64 (n,) CUDA tensors."""
+    torch = _torch()
+    if not isinstance(mat, torch.Tensor) or not mat.is_cuda or mat.dtype != torch.float32 or mat.dim() != 2 or \
+            mat.shape[0] != mat.shape[1] or not mat.is_contiguous():
+        raise TypeError("mat must be a contiguous square float32 CUDA tensor")
+    n = mat.shape[0]
+    st = _capi.lib().psdgb_composite_auto_scale_f32(
+        int(precision), int(schedule), ctypes.c_void_p(mat.data_ptr()), n, int(max_iter), float(tol), int(seed),
+        int(residual), ctypes.c_void_p(warm_start.data_ptr()) if warm_start is not None else None,
+        ctypes.c_void_p(ritz_out.data_ptr()) if ritz_out is not None else None, None, 0, None, 0,
+        _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite_auto_scale_f32")

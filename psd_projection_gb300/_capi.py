@@ -100,6 +100,8 @@ SIGNATURES = {
                                          c_vp, c_vp]),
     "psdgb_composite_auto_scale_deflate": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_dbl, c_u64, c_vp]),
     "psdgb_selftest_wait_timeout": (c_int, [c_dbl, c_vp]),
+    "psdgb_composite_auto_scale_f32": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_dbl, c_u64, c_int, c_vp, c_vp,
+                                               c_vp, c_size, c_vp, c_size, c_vp]),
     "psdgb_lobpcg": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_int, c_int, c_dbl, c_u64, c_vp, c_vp]),
     "psdgb_eig_FP64_deflate": (c_int, [c_vp, c_i64, c_i64, c_int, c_dbl, c_u64, c_vp]),
     "psdgb_composite_auto_scale_deflate_two_ends": (c_int, [c_int, c_int, c_vp, c_i64, c_i64, c_int, c_dbl, c_u64,

@@ -393,6 +393,25 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
                              d_lanczos, static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out, -1, 0);
 }
 
+psdgb_status psdgb_composite_auto_scale_f32(int precision, int schedule, float* d_mat, int64_t n, int64_t max_iter,
+                                            double tol, uint64_t seed, int residual_mode, const double* d_warm_start,
+                                            double* d_ritz_out, void* d_ws, size_t ws_bytes, void* d_lanczos,
+                                            size_t lanczos_bytes, void* stream) {
+    std::lock_guard<std::recursive_mutex> call(g_call_mu);
+    if (n < 0 || max_iter < 0) { set_error("n and max_iter must be >= 0"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    if (n == 0) return PSDGB_OK;
+    if (d_mat == nullptr) { set_error("null matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    DeviceState* ds = nullptr;
+    PSDGB_TRY(device_state(&ds));
+    PSDGB_TRY(require_sm103(ds));
+    void* ws = nullptr;
+    PSDGB_TRY(resolve_ws(ds, n, precision, d_ws, ws_bytes, &ws));
+    void* lz = d_lanczos;
+    if (lz == nullptr || lanczos_bytes < lanczos_state_bytes(n, max_iter)) PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
+    return composite_enqueue_f32(ds, precision, schedule, d_mat, n, ws, max_iter, tol, seed, residual_mode, lz,
+                                 static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out);
+}
+
 psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_schedule, int refine_precision,
                                               int refine_steps, double* d_mat, int64_t n, void* stream) {
     std::lock_guard<std::recursive_mutex> call(g_call_mu);

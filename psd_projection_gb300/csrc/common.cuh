@@ -75,7 +75,8 @@ __device__ __forceinline__ void split_store(const SplitMat& m, int fmt, size_t i
 enum EpiKind : int {
     EPI_STORE = 0,  // C -> out (split)
     EPI_STEP = 1,   // a*A + b*A3 + c*acc -> out (split); A, A3 read from split matrices
-    EPI_FINAL = 2   // 0.5*(X + up*acc) -> out64 (FP64, n x n, ld n); X read from x64
+    EPI_FINAL = 2,  // 0.5*(X + up*acc) -> out64 (FP64, n x n, ld n); X read from x64
+    EPI_FINAL32 = 3 // the same with X read from x32 and written to out32 (FP32), arithmetic in FP64
 };
 
 struct EpiParams {
@@ -91,6 +92,8 @@ struct EpiParams {
     SplitMat A3;
     const double* x64;  // EPI_FINAL input X (n x n)
     double* out64;      // EPI_FINAL output (may alias x64)
+    const float* x32;   // EPI_FINAL32 input X (n x n)
+    float* out32;       // EPI_FINAL32 output (may alias x32)
     int dual;           // mainloop: accumulate P*Q^T + Q*P^T (K doubled), the symmetric part of the product
     float acc_scale;    // the accumulator is multiplied by this first (0.5 for a dual product)
     int ld;             // row stride of the split-matrix layout (elements); np for a single matrix

@@ -299,6 +299,44 @@ psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedu
     return run_final(ds, precision, L, mat, n, nullptr, nullptr, s, scale);
 }
 
+// The auto-scaled projection of a column-major FP32 matrix, in place (its
+// upper triangle defines it): the FP32 copy for the bound comes from the FP32
+// input, the final operand split reads it, and the final epilogue writes
+// FP32 (its arithmetic in FP64).  Asynchronous, like composite_enqueue.
+psdgb_status composite_enqueue_f32(DeviceState* ds, int precision, int schedule, float* mat, int64_t n, void* ws,
+                                   int64_t max_iter, double tol, uint64_t seed, int residual_mode, void* lz_state,
+                                   cudaStream_t s, const double* d_warm, double* d_ritz_out) {
+    PSDGB_TRY(check_n(n));
+    PrecisionInfo pi{};
+    if (!precision_info(precision, &pi) || precision == PSDGB_PREC_FP32_SIMT) {
+        set_error("FP32 input needs a tensor-core precision");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
+        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (n == 0) return PSDGB_OK;
+    const Layout L = make_layout(ws, pi.fmt, n);
+    PSDGB_CUDA_TRY(launch_sym_upper_f32_to_f32(mat, n, L.a32, L.ld, s));
+    PSDGB_TRY(lanczos_bound_async(ds, L.a32, n, L.ld, max_iter, tol, seed, residual_mode, lz_state, s, d_warm,
+                                  d_ritz_out));
+    const double* up_dev = lanczos_scale_ptr(lz_state, n, max_iter);
+    const double* inv_up_dev = lanczos_inv_scale_ptr(lz_state, n, max_iter);
+    PSDGB_CUDA_TRY(launch_split_from_f32(L.a32, n, L.ld, 1.0, inv_up_dev, L.A, L.fmt, L.np, s));
+    PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s, -1, 0));
+    PSDGB_CUDA_TRY(launch_split_from_f32_upper(mat, n, 1.0, inv_up_dev, L.A2, L.fmt, L.np, s));
+    EpiParams ef = epi_base(L, n);
+    ef.kind = EPI_FINAL32;
+    ef.up = 1.0;
+    ef.up_dev = up_dev;
+    ef.dual = 1;
+    ef.acc_scale = 0.5f;
+    ef.x32 = mat;
+    ef.out32 = mat;
+    return gemm_symmetric(ds, precision, L.A2, L.A, L.np, ef, s);
+}
+
 psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                            bool auto_scale, int64_t max_iter, double tol, uint64_t seed, int residual_mode,
                            void* lz_state, cudaStream_t s, double* up_out) {

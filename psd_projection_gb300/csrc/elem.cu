@@ -19,8 +19,8 @@ constexpr int TR = 8;   // rows per thread pass
 // output tile at a time.  The output tile (bi, bj) covers rows i in
 // [32 bi, 32 bi + 32) and columns j in [32 bj, 32 bj + 32) of the row-major
 // result; the input is read coalesced through a shared-memory transpose.
-template <class Store>
-__global__ void sym_upper_tiles(const double* __restrict__ x, int64_t n, int64_t rows_out, int64_t cols_out,
+template <class T, class Store>
+__global__ void sym_upper_tiles(const T* __restrict__ x, int64_t n, int64_t rows_out, int64_t cols_out,
                                 double scale, const double* scale_dev, Store st) {
     __shared__ double sm[TS][TS + 1];
     if (scale_dev != nullptr) scale *= *scale_dev;
@@ -32,7 +32,7 @@ __global__ void sym_upper_tiles(const double* __restrict__ x, int64_t n, int64_t
     const int64_t cbase = (bi <= bj) ? bj * TS : bi * TS;  // column range of x read (c)
     for (int ty = ty0; ty < TS; ty += TR) {
         const int64_t r = rbase + tx, c = cbase + ty;
-        sm[ty][tx] = (r < n && c < n) ? x[r + c * n] : 0.0;  // sm[ty][tx] = X(rbase+tx, cbase+ty)
+        sm[ty][tx] = (r < n && c < n) ? static_cast<double>(x[r + c * n]) : 0.0;  // X(rbase+tx, cbase+ty)
     }
     __syncthreads();
     for (int ty = ty0; ty < TS; ty += TR) {
@@ -140,7 +140,24 @@ inline unsigned grid_for(int64_t count, int threads) {
 cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     dim3 block(TS, TR), grid(static_cast<unsigned>((ld + TS - 1) / TS), static_cast<unsigned>((n + TS - 1) / TS));
-    sym_upper_tiles<StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
+    sym_upper_tiles<double, StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sym_upper_f32_to_f32(const float* x, int64_t n, float* a32, int64_t ld, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    dim3 block(TS, TR), grid(static_cast<unsigned>((ld + TS - 1) / TS), static_cast<unsigned>((n + TS - 1) / TS));
+    sym_upper_tiles<float, StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
+    count_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split_from_f32_upper(const float* x, int64_t n, double scale, const double* scale_dev,
+                                        const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
+    dim3 block(TS, TR), grid(static_cast<unsigned>((np + TS - 1) / TS), static_cast<unsigned>((np + TS - 1) / TS));
+    sym_upper_tiles<float, StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev,
+                                                              StoreSplit{out, fmt, np});
     count_launch();
     return cudaGetLastError();
 }
@@ -155,7 +172,8 @@ cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, doubl
 cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const double* scale_dev,
                                         const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
     dim3 block(TS, TR), grid(static_cast<unsigned>((np + TS - 1) / TS), static_cast<unsigned>((np + TS - 1) / TS));
-    sym_upper_tiles<StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev, StoreSplit{out, fmt, np});
+    sym_upper_tiles<double, StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev,
+                                                               StoreSplit{out, fmt, np});
     count_launch();
     return cudaGetLastError();
 }

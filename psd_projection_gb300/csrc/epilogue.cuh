@@ -38,6 +38,17 @@ __device__ __forceinline__ void epi_element(const EpiParams& ep, int64_t p, int6
         }
         return;
     }
+    if (ep.kind == EPI_FINAL32) {
+        if (p < ep.n) {
+            const int64_t n = ep.n;
+            const double up = ep.up_dev ? ep.up * *ep.up_dev : ep.up;
+            const float v = static_cast<float>(
+                0.5 * (static_cast<double>(ep.x32[p * n + q]) + up * static_cast<double>(ep.acc_scale * acc)));
+            ep.out32[p * n + q] = v;
+            if (p != q) ep.out32[q * n + p] = v;
+        }
+        return;
+    }
     const size_t i0 = static_cast<size_t>(p) * ep.np + q;
     const float v = epi_value(ep, i0, acc);
     split_store(ep.out, ep.fmt, i0, v);

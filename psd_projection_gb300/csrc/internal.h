@@ -73,6 +73,11 @@ size_t split_matrix_bytes(int fmt, int64_t np);
 cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s);
 // out (Np x Np split matrix) = split(scale * (*scale_dev) * a32), zero padding
 // (scale_dev may be null: factor 1).
+// FP32 input variants: the FP32 copy of a column-major FP32 matrix's upper
+// triangle, and the split of it (scaled) into operand terms.
+cudaError_t launch_sym_upper_f32_to_f32(const float* x, int64_t n, float* a32, int64_t ld, cudaStream_t s);
+cudaError_t launch_split_from_f32_upper(const float* x, int64_t n, double scale, const double* scale_dev,
+                                        const SplitMat& out, int fmt, int64_t np, cudaStream_t s);
 cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const double* scale_dev,
                                   const SplitMat& out, int fmt, int64_t np, cudaStream_t s);
 // out (Np x Np split matrix) = split(scale * (*scale_dev) * sym_upper(x)), zero padding.
@@ -151,6 +156,9 @@ psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, dou
                                int bulk_precision, int refine_steps);
 psdgb_status composite_enqueue_scaled(DeviceState* ds, int precision, int schedule, double* mat, int64_t n, void* ws,
                                       double scale, cudaStream_t s);
+psdgb_status composite_enqueue_f32(DeviceState* ds, int precision, int schedule, float* mat, int64_t n, void* ws,
+                                   int64_t max_iter, double tol, uint64_t seed, int residual_mode, void* lz_state,
+                                   cudaStream_t s, const double* d_warm, double* d_ritz_out);
 
 // ---- eigenpairs and deflation (eigenpairs.cu) -----------------------------------
 // X += sum_i coef_i v_i v_i^T (column-major n x n; V n x r column-major; coef on the device).

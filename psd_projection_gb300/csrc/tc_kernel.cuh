@@ -247,6 +247,22 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
         }
         return;
     }
+    if (ep.kind == EPI_FINAL32) {  // FP32 input and output (single matrices only)
+        const int64_t n = ti.blk.n;
+        if (p >= n) return;
+        const double up = ti.blk.up_dev ? ep.up * *ti.blk.up_dev : ep.up;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+            const int64_t q = q0 + j;
+            if (q <= p && q < n) {
+                const float o = static_cast<float>(
+                    0.5 * (static_cast<double>(ep.x32[p * n + q]) + up * static_cast<double>(ep.acc_scale * v[j])));
+                ep.out32[p * n + q] = o;
+                if (q != p) ep.out32[q * n + p] = o;
+            }
+        }
+        return;
+    }
     const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;

@@ -343,3 +343,45 @@ def test_default_large_path_matches_evd(psd, precision):
     finally:
         psd.set_product_tuning(psd.TUNE_WIDE_KBLOCK, prev)
     assert np.linalg.norm(other - out) <= (1e-3 if precision == "fp16" else 2e-5) * np.linalg.norm(out)
+
+
+@pytest.mark.parametrize("precision", ["fp16x3", "fp16"])
+@pytest.mark.parametrize("n", [300, 2100])
+def test_f32_io_matches_f64_path(psd, precision, n):
+    """FP32 in / FP32 out (psdgb_composite_auto_scale_f32) on an input exact in
+    FP32: the same bound, filter and reconstruction as the FP64 path, whose
+    result it returns rounded to FP32 (rel. difference <= 3e-7); the lower
+    triangle is ignored (upper-triangle semantics, as the FP64 path)."""
+    import torch
+
+    x = uniform_spectrum(n, 3.0, seed=70 + n).astype(np.float32).astype(np.float64)
+    ref, _ = run(psd, x, precision, auto_scale=True)
+    garbage = np.triu(x) + np.tril(np.full_like(x, 7.0), -1)  # column-major upper triangle = row-major lower
+    t = torch.from_numpy(np.ascontiguousarray(garbage.T).astype(np.float32)).cuda()
+    s = psd.SCHEDULE_FP16 if precision == "fp16" else psd.SCHEDULE_FP32
+    psd.composite_f32(t, psd.PRECISIONS[precision], s)
+    torch.cuda.synchronize()
+    assert psd._capi.lib().psdgb_check_device_error() == 0
+    out = t.cpu().numpy().T.astype(np.float64)
+    assert np.linalg.norm(out - ref) <= 3e-7 * np.linalg.norm(ref)
+
+
+def test_f32_io_warm_start(psd):
+    import torch
+
+    n = 400
+    x = uniform_spectrum(n, 2.0, seed=81).astype(np.float32)
+    ritz = torch.empty(n, dtype=torch.float64, device="cuda")
+    t = torch.from_numpy(x).cuda()
+    psd.composite_f32(t, ritz_out=ritz)
+    e = np.random.default_rng(82).standard_normal((n, n)).astype(np.float32)
+    x2 = x + 1e-2 * 0.5 * (e + e.T)
+    t2 = torch.from_numpy(x2).cuda()
+    psd.composite_f32(t2, warm_start=ritz, max_iter=10)
+    torch.cuda.synchronize()
+    proj, _ = rp.eig_psd(x2.astype(np.float64))
+    assert rp.rel_frobenius(t2.cpu().numpy().astype(np.float64), proj) <= 1e-4
+    with pytest.raises(TypeError):
+        psd.composite_f32(torch.zeros((4, 4), dtype=torch.float64, device="cuda"))
+    with pytest.raises(psd.PsdgbError, match="tensor-core"):
+        psd.composite_f32(torch.zeros((4, 4), dtype=torch.float32, device="cuda"), psd.PRECISIONS["fp32_simt"])
