@@ -225,7 +225,7 @@ def dense_equiv_flops(n: int, steps: int) -> float:
 # ---------------------------------------------------------------------------
 
 def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 4096), n_streams: int = 64,
-                  seed: int = 0, max_slots: int = 16, check_error: bool = False) -> dict:
+                  seed: int = 0, max_slots: int = 16, check_error: bool = False, admission: str = "fifo") -> dict:
     """Closed-loop ADMM streams: stream k (n = sizes[k % 4]) waits an
     exponential think time (mean n_streams / offered_rate), perturbs its
     matrix by 1e-2 (E + E^T)/2, submits it, and waits for the projection
@@ -251,7 +251,7 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
     torch.cuda.synchronize()
     mean_think = n_streams / offered_rate
     lat, lat_by_n, gpu_ms = [], {n: [] for n in sizes}, []
-    with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10) as srv:
+    with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10, admission=admission) as srv:
         # warm the per-(slot, n) graphs outside the measured window
         for k in range(min(n_streams, 2 * len(sizes))):
             srv.submit(k, mats[k], outs[k])
@@ -298,7 +298,8 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
                 errs[ns[k]] = psd.rel_frobenius(outs[k], ref)
             err = errs
     a = np.array(lat) * 1e3
-    return {"offered_req_s": offered_rate, "throughput_req_s": completed / wall, "completed": completed,
+    return {"offered_req_s": offered_rate, "admission": admission, "throughput_req_s": completed / wall,
+            "completed": completed,
             "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
             "p99_ms": float(np.percentile(a, 99)) if len(a) else None,
             "p50_ms_by_n": {str(n): float(np.percentile(np.array(v) * 1e3, 50)) for n, v in lat_by_n.items() if v},
@@ -752,6 +753,7 @@ def run_ours(args, rank, world):
 
     if not args.no_serve:
         sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
+        sessions += [serve_session(r, args.serve_seconds, admission="shortest_first") for r in (500.0, 2000.0)]
         out["serving"] = {
             "workload": "64 closed-loop ADMM-like streams, n uniform over {64,256,1024,4096} (16 streams each), "
                         "next matrix = previous + 1e-2 (E+E^T)/2, exponential think time for the offered rate; "

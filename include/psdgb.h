@@ -228,7 +228,12 @@ typedef struct psdgb_server_config {
     int64_t max_iter;         /* Lanczos steps from the seeded start (reference default 20) */
     int64_t warm_max_iter;    /* Lanczos steps from a key's previous Ritz vector */
     int use_graphs;           /* capture each (slot, n) projection once and replay it */
+    int admission;            /* PSDGB_ADMIT_FIFO: queued requests start in submission order (a request
+                                 that does not fit the budget yet is skipped); PSDGB_ADMIT_SHORTEST_FIRST:
+                                 among each key's oldest queued request, the smallest n starts first
+                                 (ties by submission).  Both keep every key's requests in order. */
 } psdgb_server_config;
+enum { PSDGB_ADMIT_FIFO = 0, PSDGB_ADMIT_SHORTEST_FIRST = 1 };
 
 typedef struct psdgb_completion {
     uint64_t ticket;

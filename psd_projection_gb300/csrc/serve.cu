@@ -11,7 +11,10 @@
 //     requests of different sizes run concurrently on the GPU;
 //   * admission by HBM budget — a queued request starts when a slot is free
 //     and the slot's buffers for its n fit the budget (slots re-size on
-//     demand); requests that do not fit wait while smaller ones start;
+//     demand); requests that do not fit wait while smaller ones start; in
+//     submission order, or shortest first (smallest n among each key's
+//     oldest queued request), which keeps small requests' latency low when
+//     large ones saturate the GPU;
 //   * per-key order and warm starts — requests with the same key (one ADMM
 //     stream) run in submission order, and each starts its Lanczos bound from
 //     the previous request's Ritz vector, kept on the device (with
@@ -23,6 +26,7 @@
 // Every request's result depends only on its input and its key's previous
 // request: kernels are deterministic and a slot's buffers are private while
 // it runs, so a result is the same alone and in any mix.
+#include <algorithm>
 #include <chrono>
 #include <deque>
 #include <map>
@@ -208,10 +212,65 @@ psdgb_status launch_request(psdgb_server* s, Slot& sl, const Request& r) {
     return PSDGB_OK;
 }
 
-// Start queued requests while slots and budget allow (FIFO, skipping requests
-// whose key is in flight or whose buffers do not fit yet; a later request of
-// a skipped key never overtakes it).
+// Start request r on a free slot whose buffers fit (the smallest such), else
+// on a free slot re-sized for it when the budget allows.  *started says
+// whether it started; *no_slot that every slot is busy.
+psdgb_status try_start(psdgb_server* s, const Request& r, bool* started, bool* no_slot) {
+    *started = false;
+    *no_slot = false;
+    Slot* pick = nullptr;
+    for (auto& sl : s->slots)
+        if (!sl->busy && sl->cap_n >= r.n && (!pick || sl->cap_n < pick->cap_n)) pick = sl.get();
+    if (!pick) {
+        Slot* spare = nullptr;
+        for (auto& sl : s->slots)
+            if (!sl->busy && (!spare || sl->bytes < spare->bytes)) spare = sl.get();
+        if (!spare) {
+            *no_slot = true;
+            return PSDGB_OK;
+        }
+        const size_t need = slot_bytes(s->cfg, r.n) + up256(sizeof(double) * r.n);
+        if (s->used_bytes - spare->bytes + need > s->cfg.hbm_budget_bytes) return PSDGB_OK;  // not yet
+        PSDGB_TRY(slot_resize(s, *spare, r.n));
+        pick = spare;
+    }
+    PSDGB_TRY(launch_request(s, *pick, r));
+    *started = true;
+    return PSDGB_OK;
+}
+
+// Start queued requests while slots and budget allow.  FIFO: in submission
+// order, skipping requests whose key is in flight or whose buffers do not fit
+// yet (a later request of a skipped key never overtakes it).  Shortest first:
+// each key's oldest queued request is a candidate (so keys stay in order), and
+// candidates start by increasing n, ties by submission.
 psdgb_status admit(psdgb_server* s) {
+    if (s->cfg.admission == PSDGB_ADMIT_SHORTEST_FIRST) {
+        std::map<int64_t, size_t> first;  // key -> queue index of its oldest request
+        for (size_t i = 0; i < s->queue.size(); ++i)
+            if (!first.count(s->queue[i].key)) first[s->queue[i].key] = i;
+        std::vector<size_t> cand;
+        for (const auto& kv : first)
+            if (!s->keys[kv.first].busy) cand.push_back(kv.second);
+        std::sort(cand.begin(), cand.end(), [&](size_t a, size_t b) {
+            const Request &ra = s->queue[a], &rb = s->queue[b];
+            return ra.n != rb.n ? ra.n < rb.n : ra.ticket < rb.ticket;
+        });
+        std::vector<uint64_t> done;
+        for (size_t i : cand) {
+            bool started = false, no_slot = false;
+            PSDGB_TRY(try_start(s, s->queue[i], &started, &no_slot));
+            if (no_slot) break;
+            if (started) done.push_back(s->queue[i].ticket);
+        }
+        for (uint64_t tk : done)
+            for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+                if (it->ticket == tk) {
+                    s->queue.erase(it);
+                    break;
+                }
+        return PSDGB_OK;
+    }
     std::map<int64_t, bool> blocked_keys;
     for (auto it = s->queue.begin(); it != s->queue.end();) {
         const Request r = *it;
@@ -220,25 +279,14 @@ psdgb_status admit(psdgb_server* s) {
             ++it;
             continue;
         }
-        // A free slot whose buffers already fit, else any free slot to re-size.
-        Slot* pick = nullptr;
-        for (auto& sl : s->slots)
-            if (!sl->busy && sl->cap_n >= r.n && (!pick || sl->cap_n < pick->cap_n)) pick = sl.get();
-        if (!pick) {
-            Slot* spare = nullptr;
-            for (auto& sl : s->slots)
-                if (!sl->busy && (!spare || sl->bytes < spare->bytes)) spare = sl.get();
-            if (!spare) break;  // every slot is busy
-            const size_t need = slot_bytes(s->cfg, r.n) + up256(sizeof(double) * r.n);
-            if (s->used_bytes - spare->bytes + need > s->cfg.hbm_budget_bytes) {
-                blocked_keys[r.key] = true;  // does not fit now; smaller requests may
-                ++it;
-                continue;
-            }
-            PSDGB_TRY(slot_resize(s, *spare, r.n));
-            pick = spare;
+        bool started = false, no_slot = false;
+        PSDGB_TRY(try_start(s, r, &started, &no_slot));
+        if (no_slot) break;  // every slot is busy
+        if (!started) {
+            blocked_keys[r.key] = true;  // does not fit now; smaller requests may
+            ++it;
+            continue;
         }
-        PSDGB_TRY(launch_request(s, *pick, r));
         it = s->queue.erase(it);
     }
     return PSDGB_OK;
@@ -251,7 +299,8 @@ extern "C" {
 double psdgb_clock_seconds(void) { return now_s(); }
 
 psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** out) {
-    if (!cfg || !out || cfg->max_slots <= 0 || cfg->max_slots > 256 || cfg->max_iter < 0 || cfg->warm_max_iter < 0) {
+    if (!cfg || !out || cfg->max_slots <= 0 || cfg->max_slots > 256 || cfg->max_iter < 0 || cfg->warm_max_iter < 0 ||
+        (cfg->admission != PSDGB_ADMIT_FIFO && cfg->admission != PSDGB_ADMIT_SHORTEST_FIRST)) {
         set_error("psdgb_server_create: bad configuration");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }

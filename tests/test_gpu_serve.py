@@ -32,14 +32,14 @@ def _streams(sizes, steps, seed=0):
     return seqs
 
 
-def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_iter=10):
+def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_iter=10, admission="fifo"):
     import torch
 
     from psd_projection_gb300.serve import Server
 
     outs = {}
     with Server(hbm_budget_bytes=budget, max_slots=max_slots, use_graphs=use_graphs,
-                warm_max_iter=warm_max_iter) as srv:
+                warm_max_iter=warm_max_iter, admission=admission) as srv:
         ins = {}
         order = []
         steps = len(seqs[0])
@@ -104,3 +104,30 @@ def test_oversized_request_is_refused():
         x = torch.zeros((512, 512), dtype=torch.float64, device="cuda")
         with pytest.raises(PsdgbError, match="budget"):
             srv.submit(0, x)
+
+
+def test_shortest_first_admission_keeps_results_and_key_order():
+    """Shortest-first admission reorders requests across keys, never within a
+    key: every result equals the one-at-a-time result bit for bit, and with
+    one slot the small requests of the first wave finish before the large."""
+    seqs = _streams([1024, 64, 1024, 64, 256], steps=3, seed=4)
+    alone, _ = _serve(seqs, max_slots=1, together=False)
+    sjf, _ = _serve(seqs, max_slots=3, together=True, admission="shortest_first")
+    for kt in alone:
+        assert np.array_equal(alone[kt], sjf[kt]), kt
+    import torch
+
+    from psd_projection_gb300.serve import Server
+
+    order = []
+    with Server(max_slots=1, admission="shortest_first") as srv:
+        xs = [to_dev(seqs[k][0]) for k in range(len(seqs))]
+        for k, x in enumerate(xs):
+            srv.submit(k, x)
+        for c in srv.drain():
+            order.append(c.n)
+        torch.cuda.synchronize()
+    # the first request starts at once (the queue was empty); the rest by size
+    assert order[1:] == sorted(order[1:])
+    with pytest.raises(ValueError):
+        Server(admission="lifo")
