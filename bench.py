@@ -44,8 +44,8 @@ METRIC = "n=8192 proj/s & TC TFLOP/s vs plain FP32 at equal error; p50/p99 serve
 
 # DRAM bytes (read + write) of one product launch, from one ncu capture of the
 # same kernel on the same workload size (profiles/ holds the summary).
-TRAFFIC_PER_LAUNCH = {(8192, "fp16x3", True): 2.015e9}
-TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/tc_wide_kernel_fp16x3_n8192.md)"
+TRAFFIC_PER_LAUNCH = {(8192, "fp16x3", True): 1.67e9}
+TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/tc_pairwide_kernel_fp16x3_n8192.md)"
 
 
 def parse_args():
@@ -643,7 +643,8 @@ def run_ours(args, rank, world):
     peak = peaks["bf16_tflops_sustained"]
     np_ = -(-n // 128) * 128
     wide = args.precision in ("fp16", "bf16", "fp16x3", "bf16x3") and np_ >= 2048
-    kernel = (f"tc_wide_kernel (128x256 tiles, {args.precision} split operands, K chunks summed in FP32 registers)"
+    kernel = (f"tc_pairwide_kernel (256x256 tiles on CTA pairs, tcgen05.mma.cta_group::2, {args.precision} split "
+              "operands, K chunks summed in FP32 registers)"
               if wide else f"tc_group_kernel (128x128 tiles, {args.precision} split operands)")
     roofline = {
         "bound": "tensor", "kernel": kernel,
@@ -654,7 +655,7 @@ def run_ours(args, rank, world):
         "flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms, "launches": pl.value,
         "flops_counted": "MMA flops of the lower-triangle 128x128 tiles: term products x 2 x 128 x 128 x K "
                          "per tile (K doubled for the final dual product); the 1.5 % of above-diagonal work the "
-                         "128x256 tiles also do is not counted",
+                         "256x256 tiles also do is not counted",
         "share_of_step": (pms.value / ms_total) if ms_total else None,
         "traffic": TRAFFIC_PER_LAUNCH.get((n, args.precision, wide)),
         "traffic_source": TRAFFIC_SOURCE if (n, args.precision, wide) in TRAFFIC_PER_LAUNCH else None,

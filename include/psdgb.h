@@ -367,18 +367,22 @@ int psdgb_set_product_config(int acc_mode);
  *                          which sets how many operand row blocks the tiles
  *                          running at the same time share in L2; 0..64;
  *   PSDGB_TUNE_TILE_SHAPE  tile of single-matrix products: -1 = automatic
- *                          (default: 128 x 256 for one- and two-term
+ *                          (default: 256 x 256 pairs for one- and two-term
  *                          precisions at n > 1920, else 128 x 128); 0 = one
  *                          CTA per 128 x 128 tile; 1 = a CTA pair per
  *                          256 x 128 tile (one tcgen05 MMA over two SMs, each
  *                          supplying half of the B operand); 2 = one CTA per
  *                          128 x 256 tile, K accumulated in chunks summed in
  *                          FP32 registers (one- and two-term precisions; the
- *                          three-term ones keep 128 x 128);
- *   PSDGB_TUNE_WIDE_KBLOCK K block of a pipeline stage of the 128 x 256 tiles:
- *                          0 = by precision (default: 32 for two-term, 64 for
- *                          one-term products), 64 (128-byte rows) or 32
- *                          (64-byte rows, twice the stages);
+ *                          three-term ones keep 128 x 128); 3 = a CTA pair per
+ *                          256 x 256 tile (one 256 x 256 x 16 MMA over two
+ *                          SMs, K chunks summed in registers, one- and two-term
+ *                          precisions);
+ *   PSDGB_TUNE_WIDE_KBLOCK K block of a pipeline stage of the 128 x 256 and
+ *                          256 x 256 tiles: 0 = by kernel (128 x 256: 32 for
+ *                          two-term, 64 for one-term products; 256 x 256: 64),
+ *                          64 (128-byte rows) or 32 (64-byte rows, twice the
+ *                          stages);
  *   PSDGB_TUNE_GROUP_EPI_WARPS  epilogue warps of the 128 x 128 kernel when it
  *                          runs four accumulator buffers (short K: batches and
  *                          small matrices): 4 or 8. */

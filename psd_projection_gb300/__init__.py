@@ -292,7 +292,7 @@ TUNE_TILE_GROUP = 1
 TUNE_TILE_SHAPE = 2
 TUNE_WIDE_KBLOCK = 3
 TUNE_GROUP_EPI_WARPS = 4
-TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256 = -1, 0, 1, 2
+TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256, TILE_PAIR_256X256 = -1, 0, 1, 2, 3
 
 
 def set_product_config(acc_mode: int) -> int:

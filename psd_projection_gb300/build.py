@@ -26,7 +26,7 @@ CFLAGS = [
     "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
 ]
-SOURCES = ["capi.cu", "composite.cu", "elem.cu", "lanczos.cu", "gemm_simt.cu", "gemm_tc.cu", "gemm_tc2.cu", "gemm_wide.cu", "eigenpairs.cu", "lobpcg.cu", "refapi.cu",
+SOURCES = ["capi.cu", "composite.cu", "elem.cu", "lanczos.cu", "gemm_simt.cu", "gemm_tc.cu", "gemm_tc2.cu", "gemm_wide.cu", "gemm_pairwide.cu", "eigenpairs.cu", "lobpcg.cu", "refapi.cu",
            "static_scratch.cu", "serve.cu", "batch.cu"]
 
 

@@ -850,7 +850,7 @@ int psdgb_set_product_tuning(int knob, int value) {
         }
         case PSDGB_TUNE_TILE_SHAPE: {
             const int prev = g_tile_shape;
-            if (value >= -1 && value <= TILE_WIDE_128X256) g_tile_shape = value;
+            if (value >= -1 && value <= TILE_PAIR_256X256) g_tile_shape = value;
             return prev;
         }
         case PSDGB_TUNE_GROUP_EPI_WARPS: {

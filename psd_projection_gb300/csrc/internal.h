@@ -108,9 +108,10 @@ extern int g_single_acc_mode;  // forced configuration of single-matrix products
 int auto_acc_mode(int precision, int64_t np);
 // Tile shape of single-matrix products: one CTA per 128 x 128 tile (gemm_tc.cu),
 // a CTA pair per 256 x 128 tile (gemm_tc2.cu), one CTA per 128 x 256 tile
-// (gemm_wide.cu; one- and two-term precisions, others use 128 x 128); -1
-// chooses: 128 x 256 for one- and two-term precisions at np >= 2048.
-enum TileShape : int { TILE_128X128 = 0, TILE_PAIR_256X128 = 1, TILE_WIDE_128X256 = 2 };
+// (gemm_wide.cu; one- and two-term precisions, others use 128 x 128), a CTA
+// pair per 256 x 256 tile (gemm_pairwide.cu; one- and two-term precisions);
+// -1 chooses: 256 x 256 pairs for one- and two-term precisions at np >= 2048.
+enum TileShape : int { TILE_128X128 = 0, TILE_PAIR_256X128 = 1, TILE_WIDE_128X256 = 2, TILE_PAIR_256X256 = 3 };
 extern int g_tile_shape;
 extern int g_group_epi_warps;  // epilogue warps of 128 x 128 tiles with four accumulator buffers: 4 or 8
 extern int g_wide_kblock;  // K block of the 128 x 256 kernel: 64, 32, or 0 (by precision)
@@ -119,6 +120,9 @@ extern int g_tile_group_rows;  // tile order of single-matrix products (grouped_
 // tcgen05.mma.cta_group::2 per term product and K slice; np >= 256.
 psdgb_status gemm_tc_pair(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
                           int64_t np, const EpiParams& ep, cudaStream_t s);
+// One matrix on CTA pairs with 256 x 256 tiles (gemm_pairwide.cu): one- and two-term precisions.
+psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                              const EpiParams& ep, cudaStream_t s);
 // One matrix on 128 x 256 tiles (gemm_wide.cu): one- and two-term precisions; np >= 256.
 psdgb_status gemm_tc_wide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                           const EpiParams& ep, cudaStream_t s);

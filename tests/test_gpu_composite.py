@@ -385,3 +385,23 @@ def test_f32_io_warm_start(psd):
         psd.composite_f32(torch.zeros((4, 4), dtype=torch.float64, device="cuda"))
     with pytest.raises(psd.PsdgbError, match="tensor-core"):
         psd.composite_f32(torch.zeros((4, 4), dtype=torch.float32, device="cuda"), psd.PRECISIONS["fp32_simt"])
+
+
+@pytest.mark.parametrize("precision", ["fp16x3", "bf16x3", "fp16"])
+@pytest.mark.parametrize("n", [300, 513, 1000, 2100])
+def test_pair_wide_tiles_match_wide(psd, precision, n):
+    """256 x 256 tiles on CTA pairs (one cta_group::2 MMA of 256 x 256 x 16
+    over two SMs) against 128 x 256 tiles on one CTA: the same term products
+    and K chunks, so the same projection (relative difference <= 1e-6), within
+    the bars of the FP64 EVD projection."""
+    x = uniform_spectrum(n, 2.0, seed=90 + n)
+    proj, _ = rp.eig_psd(x)
+    prev = psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_WIDE_128X256)
+    try:
+        wide, _ = run(psd, x, precision, auto_scale=True)
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_PAIR_256X256)
+        pair, _ = run(psd, x, precision, auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, prev)
+    assert np.linalg.norm(pair - wide) <= 1e-6 * np.linalg.norm(wide)
+    assert rp.rel_frobenius(pair, proj) <= (2e-3 if precision == "fp16" else 1e-4)
