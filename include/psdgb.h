@@ -385,12 +385,18 @@ int psdgb_set_product_config(int acc_mode);
  *                          stages);
  *   PSDGB_TUNE_GROUP_EPI_WARPS  epilogue warps of the 128 x 128 kernel when it
  *                          runs four accumulator buffers (short K: batches and
- *                          small matrices): 4 or 8. */
+ *                          small matrices): 4 or 8;
+ *   PSDGB_TUNE_LANCZOS_SYMV  matvec of the Lanczos bound: -1 = automatic
+ *                          (default: the lower block triangle in 128 x 128
+ *                          tiles from n = 2048), 0 = the whole matrix, a warp
+ *                          per column, 1 = the triangle tiles for n >= 128
+ *                          (16 consumer warps), 2 = the same with 8. */
 enum {
     PSDGB_TUNE_TILE_GROUP = 1,
     PSDGB_TUNE_TILE_SHAPE = 2,
     PSDGB_TUNE_WIDE_KBLOCK = 3,
-    PSDGB_TUNE_GROUP_EPI_WARPS = 4
+    PSDGB_TUNE_GROUP_EPI_WARPS = 4,
+    PSDGB_TUNE_LANCZOS_SYMV = 5
 };
 int psdgb_set_product_tuning(int knob, int value);
 

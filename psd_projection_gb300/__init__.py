@@ -292,6 +292,7 @@ TUNE_TILE_GROUP = 1
 TUNE_TILE_SHAPE = 2
 TUNE_WIDE_KBLOCK = 3
 TUNE_GROUP_EPI_WARPS = 4
+TUNE_LANCZOS_SYMV = 5
 TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256, TILE_PAIR_256X256 = -1, 0, 1, 2, 3
 
 
@@ -301,8 +302,11 @@ def set_product_config(acc_mode: int) -> int:
 
 
 def set_product_tuning(knob: int, value: int) -> int:
-    """TUNE_TILE_GROUP (tile rows per group of the tile order, 0 = row by row) or TUNE_TILE_SHAPE
-    (TILE_AUTO, TILE_128X128, TILE_PAIR_256X128, TILE_WIDE_128X256); returns the previous value."""
+    """Process-wide product / bound settings; returns the previous value.  TUNE_TILE_GROUP (tile rows
+    per group of the tile order, 0 = row by row), TUNE_TILE_SHAPE (TILE_AUTO, TILE_128X128,
+    TILE_PAIR_256X128, TILE_WIDE_128X256, TILE_PAIR_256X256), TUNE_WIDE_KBLOCK (0, 32, 64),
+    TUNE_GROUP_EPI_WARPS (4, 8), TUNE_LANCZOS_SYMV (-1 automatic, 0 whole-matrix matvec, 1 lower
+    block triangle)."""
     return int(_capi.lib().psdgb_set_product_tuning(int(knob), int(value)))
 
 

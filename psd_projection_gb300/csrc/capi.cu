@@ -184,9 +184,19 @@ psdgb_status require_sm103(DeviceState* ds) {
     return PSDGB_OK;
 }
 
+// Caller workspaces feed TMA tensor maps and 16-byte vector accesses.
+psdgb_status check_ws_align(const void* p, const char* what) {
+    if (p != nullptr && (reinterpret_cast<uintptr_t>(p) & 15u) != 0) {
+        set_error(std::string(what) + " must be 16-byte aligned (cudaMalloc gives 256)");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    return PSDGB_OK;
+}
+
 // Resolve the composite workspace: the caller's when large enough, else the cache.
 psdgb_status resolve_ws(DeviceState* ds, int64_t n, int precision, void* d_ws, size_t ws_bytes, void** out) {
     const size_t need = composite_ws_bytes(n, precision);
+    PSDGB_TRY(check_ws_align(d_ws, "the workspace"));
     if (d_ws != nullptr && ws_bytes >= need) {
         *out = d_ws;
         return PSDGB_OK;
@@ -386,6 +396,8 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
                   "psdgb_composite_workspace_size and psdgb_lanczos_state_size bytes");
         return PSDGB_ERR_WORKSPACE_TOO_SMALL;
     }
+    PSDGB_TRY(check_ws_align(d_ws, "the workspace"));
+    PSDGB_TRY(check_ws_align(d_lanczos, "the Lanczos state"));
     DeviceState* ds = nullptr;
     PSDGB_TRY(device_state(&ds));
     PSDGB_TRY(require_sm103(ds));
@@ -406,6 +418,7 @@ psdgb_status psdgb_composite_auto_scale_f32(int precision, int schedule, float* 
     PSDGB_TRY(require_sm103(ds));
     void* ws = nullptr;
     PSDGB_TRY(resolve_ws(ds, n, precision, d_ws, ws_bytes, &ws));
+    PSDGB_TRY(check_ws_align(d_lanczos, "the Lanczos state"));
     void* lz = d_lanczos;
     if (lz == nullptr || lanczos_bytes < lanczos_state_bytes(n, max_iter)) PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
     return composite_enqueue_f32(ds, precision, schedule, d_mat, n, ws, max_iter, tol, seed, residual_mode, lz,
@@ -476,6 +489,7 @@ psdgb_status psdgb_two_norm_ex(const double* d_A, int64_t n, double* lo, double*
         const int64_t ld = (n + 3) / 4 * 4;
         const size_t a32_bytes = sizeof(float) * static_cast<size_t>(n) * ld;
         void* a32 = nullptr;
+        PSDGB_TRY(check_ws_align(d_ws, "the workspace"));
         if (d_ws != nullptr && ws_bytes >= a32_bytes) {
             a32 = d_ws;
         } else {
@@ -861,6 +875,11 @@ int psdgb_set_product_tuning(int knob, int value) {
         case PSDGB_TUNE_WIDE_KBLOCK: {
             const int prev = g_wide_kblock;
             if (value == 0 || value == 32 || value == 64) g_wide_kblock = value;
+            return prev;
+        }
+        case PSDGB_TUNE_LANCZOS_SYMV: {
+            const int prev = g_lanczos_symv;
+            if (value >= -1 && value <= 2) g_lanczos_symv = value;
             return prev;
         }
         default: return -1;

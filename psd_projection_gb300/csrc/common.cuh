@@ -138,7 +138,8 @@ enum DeviceError : int {
     DEVERR_MMA_WAIT = 2,     // MMA warp gave up waiting for loaded operands
     DEVERR_EPI_WAIT = 3,     // epilogue gave up waiting for the accumulator
     DEVERR_DRAIN_WAIT = 4,   // in-flight copies/MMAs did not drain after an abort
-    DEVERR_SELFTEST_WAIT = 5 // the self-test's wait on a barrier nothing arrives at gave up (expected)
+    DEVERR_SELFTEST_WAIT = 5, // the self-test's wait on a barrier nothing arrives at gave up (expected)
+    DEVERR_SYMV_WAIT = 6      // the Lanczos tile matvec gave up waiting for a tile or a free stage
 };
 
 #if defined(__CUDACC__)

@@ -15,40 +15,54 @@ constexpr int TS = 32;  // transpose tile
 constexpr int TR = 8;   // rows per thread pass
 
 // Visit the symmetric matrix defined by the upper triangle of the
-// column-major x (element (r, c) at x[r + c*n], used where r <= c) one 32x32
-// output tile at a time.  The output tile (bi, bj) covers rows i in
-// [32 bi, 32 bi + 32) and columns j in [32 bj, 32 bj + 32) of the row-major
-// result; the input is read coalesced through a shared-memory transpose.
+// column-major x (element (r, c) at x[r + c*n], used where r <= c) one pair of
+// mirrored 32x32 output tiles at a time: block t reads the source tile of
+// rows [32 lo, 32 lo + 32) and columns [32 hi, 32 hi + 32) (lo <= hi) once,
+// coalesced, and writes the row-major output tiles (lo, hi) and (hi, lo)
+// through a shared-memory transpose (only (lo, lo) on the diagonal).  Each
+// upper element is read once: 4 n^2 bytes of FP64 input per matrix.
 template <class T, class Store>
-__global__ void sym_upper_tiles(const T* __restrict__ x, int64_t n, int64_t rows_out, int64_t cols_out,
-                                double scale, const double* scale_dev, Store st) {
+__global__ void __launch_bounds__(TS * TR) sym_upper_tiles(const T* __restrict__ x, int64_t n, int64_t rows_out,
+                                                           int64_t cols_out, double scale, const double* scale_dev,
+                                                           Store st) {
     __shared__ double sm[TS][TS + 1];
     if (scale_dev != nullptr) scale *= *scale_dev;
-    const int64_t bi = blockIdx.y, bj = blockIdx.x;
+    // Pair t in row-major order over the tiles (hi, lo), lo <= hi.
+    const int64_t t = blockIdx.x;
+    // FP32 square root for the estimate (FP64 issues slowly on this GPU); the
+    // integer corrections below make it exact.
+    int64_t hi = static_cast<int64_t>((sqrtf(8.0f * static_cast<float>(t) + 1.0f) - 1.0f) * 0.5f);
+    while (hi * (hi + 1) / 2 > t) --hi;
+    while ((hi + 1) * (hi + 2) / 2 <= t) ++hi;
+    const int64_t lo = t - hi * (hi + 1) / 2;
     const int tx = threadIdx.x, ty0 = threadIdx.y;
-    // Source block: columns (c) of the column-major input are the tile's j
-    // when bi <= bj, and its i when bi > bj.
-    const int64_t rbase = (bi <= bj) ? bi * TS : bj * TS;  // row range of x read (r)
-    const int64_t cbase = (bi <= bj) ? bj * TS : bi * TS;  // column range of x read (c)
+    const int64_t rbase = lo * TS, cbase = hi * TS;
     for (int ty = ty0; ty < TS; ty += TR) {
         const int64_t r = rbase + tx, c = cbase + ty;
         sm[ty][tx] = (r < n && c < n) ? static_cast<double>(x[r + c * n]) : 0.0;  // X(rbase+tx, cbase+ty)
     }
     __syncthreads();
     for (int ty = ty0; ty < TS; ty += TR) {
-        const int64_t i = bi * TS + ty, j = bj * TS + tx;
-        if (i >= rows_out || j >= cols_out) continue;
-        double v;
-        if (bi < bj) {
-            v = sm[tx][ty];                        // X(i, j), i < j
-        } else if (bi > bj) {
-            v = sm[ty][tx];                        // X(j, i), j < i
-        } else {
-            v = (ty <= tx) ? sm[tx][ty] : sm[ty][tx];  // diagonal block
+        {   // tile (lo, hi): X(i, j) with i = rbase + ty <= j = cbase + tx (or the diagonal block)
+            const int64_t i = rbase + ty, j = cbase + tx;
+            double v = (lo < hi || ty <= tx) ? sm[tx][ty] : sm[ty][tx];
+            if (i >= n || j >= n) v = 0.0;
+            if (i < rows_out && j < cols_out) st(i, j, v * scale);
         }
-        if (i >= n || j >= n) v = 0.0;
-        st(i, j, v * scale);
+        if (lo < hi) {  // tile (hi, lo): X(i, j) = X(j, i), i = cbase + ty, j = rbase + tx
+            const int64_t i = cbase + ty, j = rbase + tx;
+            double v = sm[ty][tx];
+            if (i >= n || j >= n) v = 0.0;
+            if (i < rows_out && j < cols_out) st(i, j, v * scale);
+        }
     }
+}
+
+// Blocks of the pair grid that cover a rows_out x cols_out output.
+inline unsigned pair_blocks(int64_t rows_out, int64_t cols_out) {
+    const int64_t e = rows_out > cols_out ? rows_out : cols_out;
+    const int64_t nt = (e + TS - 1) / TS;
+    return static_cast<unsigned>(nt * (nt + 1) / 2);
 }
 
 struct StoreF32 {
@@ -66,15 +80,64 @@ struct StoreSplit {
     }
 };
 
+// split_store for 8 consecutive elements (idx a multiple of 8): the same
+// arithmetic, one 16-byte store per term plane.
+__device__ __forceinline__ void split_store8(const SplitMat& m, int fmt, size_t idx, const float (&v)[8]) {
+    if (fmt == FMT_F32) {
+        float4* d = reinterpret_cast<float4*>(static_cast<float*>(m.term[0]) + idx);
+        d[0] = make_float4(v[0], v[1], v[2], v[3]);
+        d[1] = make_float4(v[4], v[5], v[6], v[7]);
+        return;
+    }
+    if (fmt == FMT_F16) {
+        __align__(16) __half h[8];
+        __align__(16) __half l[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            h[e] = __float2half_rn(v[e]);
+            l[e] = __float2half_rn(v[e] - __half2float(h[e]));
+        }
+        *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[0]) + idx) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[1]) + idx) = *reinterpret_cast<const uint4*>(l);
+        return;
+    }
+    __align__(16) __nv_bfloat16 b0[8];
+    __align__(16) __nv_bfloat16 b1[8];
+    __align__(16) __nv_bfloat16 b2[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        b0[e] = __float2bfloat16_rn(v[e]);
+        const float r1 = v[e] - __bfloat162float(b0[e]);
+        b1[e] = __float2bfloat16_rn(r1);
+        b2[e] = __float2bfloat16_rn(r1 - __bfloat162float(b1[e]));
+    }
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[0]) + idx) = *reinterpret_cast<const uint4*>(b0);
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[1]) + idx) = *reinterpret_cast<const uint4*>(b1);
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[2]) + idx) = *reinterpret_cast<const uint4*>(b2);
+}
+
+// out = split(a * scale) over the Np x Np operand (zero padding), 8 columns
+// per thread: two 16-byte loads (vec: a 16-byte aligned, ld a multiple of 4)
+// and one 16-byte store per term plane.
 __global__ void split_from_f32_kernel(const float* __restrict__ a, int64_t n, int64_t ld, double scale64,
-                                      const double* scale_dev, SplitMat out, int fmt, int64_t np) {
+                                      const double* scale_dev, SplitMat out, int fmt, int64_t np, int vec) {
     const float scale = static_cast<float>(scale_dev != nullptr ? scale64 * *scale_dev : scale64);
-    const int64_t total = np * np;
+    const int64_t chunks = np / 8;
+    const int64_t total = np * chunks;
     for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < total;
          idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int64_t p = idx / np, q = idx - p * np;
-        const float v = (p < n && q < n) ? a[p * ld + q] * scale : 0.0f;
-        split_store(out, fmt, static_cast<size_t>(idx), v);
+        const int64_t p = idx / chunks, q = (idx - p * chunks) * 8;
+        float v[8];
+        if (vec && p < n && q + 8 <= n) {
+            const float4 u0 = *reinterpret_cast<const float4*>(a + p * ld + q);
+            const float4 u1 = *reinterpret_cast<const float4*>(a + p * ld + q + 4);
+            v[0] = u0.x * scale; v[1] = u0.y * scale; v[2] = u0.z * scale; v[3] = u0.w * scale;
+            v[4] = u1.x * scale; v[5] = u1.y * scale; v[6] = u1.z * scale; v[7] = u1.w * scale;
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = (p < n && q + e < n) ? a[p * ld + q + e] * scale : 0.0f;
+        }
+        split_store8(out, fmt, static_cast<size_t>(p * np + q), v);
     }
 }
 
@@ -139,41 +202,45 @@ inline unsigned grid_for(int64_t count, int threads) {
 
 cudaError_t launch_sym_upper_to_f32(const double* x, int64_t n, float* a32, int64_t ld, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    dim3 block(TS, TR), grid(static_cast<unsigned>((ld + TS - 1) / TS), static_cast<unsigned>((n + TS - 1) / TS));
-    sym_upper_tiles<double, StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
+    const dim3 block(TS, TR);
+    sym_upper_tiles<double, StoreF32><<<pair_blocks(n, ld), block, 0, s>>>(x, n, n, ld, 1.0, nullptr,
+                                                                           StoreF32{a32, ld});
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_sym_upper_f32_to_f32(const float* x, int64_t n, float* a32, int64_t ld, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    dim3 block(TS, TR), grid(static_cast<unsigned>((ld + TS - 1) / TS), static_cast<unsigned>((n + TS - 1) / TS));
-    sym_upper_tiles<float, StoreF32><<<grid, block, 0, s>>>(x, n, n, ld, 1.0, nullptr, StoreF32{a32, ld});
+    const dim3 block(TS, TR);
+    sym_upper_tiles<float, StoreF32><<<pair_blocks(n, ld), block, 0, s>>>(x, n, n, ld, 1.0, nullptr,
+                                                                          StoreF32{a32, ld});
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_split_from_f32_upper(const float* x, int64_t n, double scale, const double* scale_dev,
                                         const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
-    dim3 block(TS, TR), grid(static_cast<unsigned>((np + TS - 1) / TS), static_cast<unsigned>((np + TS - 1) / TS));
-    sym_upper_tiles<float, StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev,
-                                                              StoreSplit{out, fmt, np});
+    const dim3 block(TS, TR);
+    sym_upper_tiles<float, StoreSplit><<<pair_blocks(np, np), block, 0, s>>>(x, n, np, np, scale, scale_dev,
+                                                                             StoreSplit{out, fmt, np});
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_split_from_f32(const float* a32, int64_t n, int64_t ld, double scale, const double* scale_dev,
                                   const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
-    split_from_f32_kernel<<<grid_for(np * np, 256), 256, 0, s>>>(a32, n, ld, scale, scale_dev, out, fmt, np);
+    const int vec = (reinterpret_cast<uintptr_t>(a32) & 15u) == 0 && ld % 4 == 0;
+    split_from_f32_kernel<<<grid_for(np * np / 8, 256), 256, 0, s>>>(a32, n, ld, scale, scale_dev, out, fmt, np,
+                                                                      vec);
     count_launch();
     return cudaGetLastError();
 }
 
 cudaError_t launch_split_from_f64_upper(const double* x, int64_t n, double scale, const double* scale_dev,
                                         const SplitMat& out, int fmt, int64_t np, cudaStream_t s) {
-    dim3 block(TS, TR), grid(static_cast<unsigned>((np + TS - 1) / TS), static_cast<unsigned>((np + TS - 1) / TS));
-    sym_upper_tiles<double, StoreSplit><<<grid, block, 0, s>>>(x, n, np, np, scale, scale_dev,
-                                                               StoreSplit{out, fmt, np});
+    const dim3 block(TS, TR);
+    sym_upper_tiles<double, StoreSplit><<<pair_blocks(np, np), block, 0, s>>>(x, n, np, np, scale, scale_dev,
+                                                                              StoreSplit{out, fmt, np});
     count_launch();
     return cudaGetLastError();
 }

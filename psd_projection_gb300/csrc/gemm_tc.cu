@@ -323,6 +323,20 @@ bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16,
     return r == CUDA_SUCCESS;
 }
 
+bool make_tmap_f32(CUtensorMap* tm, const void* base, int64_t ld, int64_t rows, int64_t cols, int box_rows,
+                   int box_cols) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(cols), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld) * 4};
+    const cuuint32_t box[2] = {static_cast<cuuint32_t>(box_cols), static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,
                            int64_t ld, int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles,
                            int grid, cudaStream_t s) {

@@ -4,6 +4,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <string>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -49,6 +50,12 @@ struct DeviceState {
 psdgb_status device_state(DeviceState** out);
 // Synchronise the stream and turn a device error word into a status.
 psdgb_status finish(DeviceState* ds, cudaStream_t stream);
+
+// FP32 row-major matrix of rows x cols (row stride ld elements, a multiple of
+// 4) as a TMA tensor map of unswizzled box_rows x box_cols tiles, zero fill
+// outside the matrix (gemm_tc.cu).
+bool make_tmap_f32(CUtensorMap* tm, const void* base, int64_t ld, int64_t rows, int64_t cols, int box_rows,
+                   int box_cols);
 
 // ---- product timing (capi.cu) --------------------------------------------------
 // Record an event before / after a product launch when timing is enabled.
@@ -116,6 +123,7 @@ extern int g_tile_shape;
 extern int g_group_epi_warps;  // epilogue warps of 128 x 128 tiles with four accumulator buffers: 4 or 8
 extern int g_wide_kblock;  // K block of the 128 x 256 kernel: 64, 32, or 0 (by precision)
 extern int g_tile_group_rows;  // tile order of single-matrix products (grouped_decode), 0 = row by row
+extern int g_lanczos_symv;  // Lanczos matvec over 128 x 128 triangle tiles: -1 automatic (n >= 2048), 0 off, 1 on
 // One matrix on CTA pairs (gemm_tc2.cu): 256 x 128 tiles, one
 // tcgen05.mma.cta_group::2 per term product and K slice; np >= 256.
 psdgb_status gemm_tc_pair(DeviceState* ds, int precision, int acc_mode, const SplitMat& P, const SplitMat& Q,

@@ -11,10 +11,16 @@
 //     :255 runs ry -> w1, leaving ry = A y); PSDGB_RESIDUAL_EXACT uses
 //     r = A^T A y - theta y instead.
 //
-// GB300 design: the matrix is streamed as FP32 (4 n^2 bytes per matvec
-// instead of the reference's 8 n^2 per Dgemv, two per step), one warp per
-// column with 128-bit loads and warp-shuffle reductions, FP64 for every
-// reduction and every vector.  The whole bound runs on the device: the
+// GB300 design: the matrix is streamed as FP32, FP64 for every vector and
+// every cross-tile sum.  From n = 2048 up each matvec reads only the lower
+// block triangle of the symmetric matrix (2 n^2 bytes instead of the
+// reference's 8 n^2 per Dgemv, two per step): 128 x 128 tiles arrive by TMA
+// in a three-stage mbarrier pipeline, and each off-diagonal tile A_ij yields
+// both A_ij x_j (row sums, for y_i) and A_ij^T x_i (column sums, for y_j).
+// The nb per-tile partial sums of a 128-row block are stored in FP64 and
+// added in a fixed order by a second small kernel, so the result does not
+// depend on scheduling.  Below n = 2048 a warp per column streams the
+// whole matrix with 128-bit loads.  The whole bound runs on the device: the
 // recurrence, the largest eigenpair of T (Sturm-sequence multisection in one
 // warp and inverse iteration, instead of the reference's cuSOLVER Dsyevd
 // with host round trips), the Ritz residual, and the scale 1/up the filter
@@ -45,7 +51,7 @@ struct LzState {
 
 // Layout of the Lanczos state inside its buffer.
 struct LzLayout {
-    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk, work;
+    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk, work, part;
     size_t total;
 };
 
@@ -69,6 +75,8 @@ LzLayout lz_layout(int64_t n, int64_t m) {
     L.u32 = take(sizeof(float) * n4);
     L.uk = take(sizeof(double) * (m + 1));
     L.work = take(sizeof(double) * 4 * (m + 1));  // tridiagonal LU of the inverse iteration
+    const size_t nb = static_cast<size_t>((n + 127) / 128);
+    L.part = take(sizeof(double) * nb * nb * 128);  // tile matvec: partial sums [row block][source block][128]
     L.total = off;
     return L;
 }
@@ -202,6 +210,228 @@ __global__ void __launch_bounds__(256) lz_matvec_kernel(const float* __restrict_
     }
 }
 
+// ---- matvec over the lower block triangle (n >= 2048) -----------------------
+constexpr int SV_T = 128;                 // tile edge
+constexpr int SV_STAGES = 3;              // TMA pipeline depth (64 KB a stage)
+constexpr int SV_CWARPS_MAX = 16;
+constexpr uint32_t SV_TILE_BYTES = SV_T * SV_T * sizeof(float);
+constexpr size_t SV_SMEM = 128 + SV_STAGES * static_cast<size_t>(SV_TILE_BYTES) +
+                           2 * SV_CWARPS_MAX * SV_T * sizeof(float) +  // column sums of the warps, two buffers
+                           2 * SV_STAGES * sizeof(uint64_t) + 16;
+
+// Barrier of the nthreads consumer threads that also ORs a predicate over
+// them (every thread gets the same answer).
+__device__ __forceinline__ bool consumer_sync_or(bool v, int nthreads) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"(static_cast<uint32_t>(v)), "r"(nthreads)
+        : "memory");
+    return r != 0;
+}
+
+// Tile t of the lower block triangle in row-major order: row block bi holds
+// tiles (bi, 0..bi).
+__device__ __forceinline__ void sv_decode(int64_t t, int& bi, int& bj) {
+    // FP32 square root for the estimate (FP64 issues slowly on this GPU); the
+    // integer corrections below make it exact.
+    int r = static_cast<int>((sqrtf(8.0f * static_cast<float>(t) + 1.0f) - 1.0f) * 0.5f);
+    while (static_cast<int64_t>(r) * (r + 1) / 2 > t) --r;
+    while (static_cast<int64_t>(r + 1) * (r + 2) / 2 <= t) ++r;
+    bi = r;
+    bj = static_cast<int>(t - static_cast<int64_t>(r) * (r + 1) / 2);
+}
+
+// Partial sums of y = A x for the symmetric FP32 matrix A (n x n, row stride
+// ld) from its lower block triangle: part[(b * nb + s) * 128 + r] receives
+// row r of row block b summed over column block s (each entry written once;
+// lz_symv_reduce_kernel adds them up).  CW consumer warps (8 or 16) and one
+// TMA warp; consumer warp w handles tile rows ROWS w .. ROWS w + ROWS - 1,
+// lane l columns 4l..4l+3; the x segments of the next tile are loaded while
+// the current one is consumed, and each tile costs its consumers one barrier.
+// With `reverse` the tiles are visited last to first: consecutive matvecs
+// alternate, so each starts on the tiles the previous one left in L2.
+template <int CW>
+__global__ void __launch_bounds__(32 * (CW + 1), 1)
+    lz_symv_kernel(const __grid_constant__ CUtensorMap tmap, int64_t n, int nb, const float* __restrict__ x,
+                   double* __restrict__ part, const int* skip, int* err, int reverse) {
+    constexpr int SV_CWARPS = CW;
+    constexpr int SV_ROWS = SV_T / CW;      // tile rows per consumer warp
+    constexpr int SV_G = 32 / SV_ROWS;      // lanes that share a row after the halving steps
+    static_assert(CW == 8 || CW == 16, "8 or 16 consumer warps");
+    if (skip != nullptr && *skip) return;
+    extern __shared__ uint8_t sv_raw[];
+    uint8_t* smem = sv_raw + ((128u - (smem_u32(sv_raw) & 127u)) & 127u);
+    float* stage = reinterpret_cast<float*>(smem);
+    float* red = stage + SV_STAGES * SV_T * SV_T;
+    uint64_t* full = reinterpret_cast<uint64_t*>(red + 2 * SV_CWARPS * SV_T);
+    uint64_t* empty = full + SV_STAGES;
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(empty + SV_STAGES);
+
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int64_t ntiles = static_cast<int64_t>(nb) * (nb + 1) / 2;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < SV_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], SV_CWARPS);
+        }
+        *abort_flag = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    int issued = 0;
+    if (warp == SV_CWARPS) {
+        // ---- TMA producer ----
+        if (lane == 0) {
+            tma_prefetch_desc(&tmap);
+            int k = 0;
+            for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+                const int s = k % SV_STAGES;
+                const uint32_t ph = static_cast<uint32_t>(k / SV_STAGES) & 1u;
+                if (!mbar_wait_bounded(&empty[s], ph ^ 1u)) {
+                    *abort_flag = 1;
+                    atomicCAS(err, 0, DEVERR_SYMV_WAIT);
+                    break;
+                }
+                if (*abort_flag) break;
+                int bi, bj;
+                sv_decode(reverse ? ntiles - 1 - t : t, bi, bj);
+                mbar_arrive_expect_tx(&full[s], SV_TILE_BYTES);
+                tma_load_2d(stage + s * SV_T * SV_T, &tmap, &full[s], bj * SV_T, bi * SV_T);
+                issued = k + 1;
+            }
+        }
+    } else {
+        // ---- consumers ----
+        const int tid = threadIdx.x;  // 0..32 CW - 1
+        // x_j for this lane's four columns and x_i for the warp's 8 rows of a
+        // tile (x_i: the same address in every lane, a broadcast load).
+        auto load_x = [&](int64_t t, float (&xj)[4], float (&xi)[SV_ROWS]) {
+            int bi, bj;
+            sv_decode(reverse ? ntiles - 1 - t : t, bi, bj);
+            const int64_t c0 = static_cast<int64_t>(bj) * SV_T + 4 * lane;
+            const int64_t r0 = static_cast<int64_t>(bi) * SV_T + SV_ROWS * warp;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) xj[e] = c0 + e < n ? __ldg(x + c0 + e) : 0.0f;
+#pragma unroll
+            for (int e = 0; e < SV_ROWS; ++e) xi[e] = r0 + e < n ? __ldg(x + r0 + e) : 0.0f;
+        };
+        float xj[4], xi[SV_ROWS], xj_n[4], xi_n[SV_ROWS];
+        if (blockIdx.x < ntiles) load_x(blockIdx.x, xj, xi);
+        int k = 0;
+        for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++k) {
+            const int s = k % SV_STAGES;
+            const uint32_t ph = static_cast<uint32_t>(k / SV_STAGES) & 1u;
+            int bi, bj;
+            sv_decode(reverse ? ntiles - 1 - t : t, bi, bj);
+            if (t + gridDim.x < ntiles) load_x(t + gridDim.x, xj_n, xi_n);
+            const bool ok = mbar_wait_bounded(&full[s], ph);
+            if (!ok && lane == 0) {
+                *abort_flag = 1;
+                atomicCAS(err, 0, DEVERR_SYMV_WAIT);
+            }
+            const float* tile = stage + s * SV_T * SV_T;
+            float cs0 = 0.f, cs1 = 0.f, cs2 = 0.f, cs3 = 0.f;
+            float rp[SV_ROWS];
+#pragma unroll
+            for (int rr = 0; rr < SV_ROWS; ++rr) {
+                const float4 a = reinterpret_cast<const float4*>(tile + (SV_ROWS * warp + rr) * SV_T)[lane];
+                cs0 = fmaf(a.x, xi[rr], cs0);
+                cs1 = fmaf(a.y, xi[rr], cs1);
+                cs2 = fmaf(a.z, xi[rr], cs2);
+                cs3 = fmaf(a.w, xi[rr], cs3);
+                rp[rr] = fmaf(a.x, xj[0], fmaf(a.y, xj[1], fmaf(a.z, xj[2], a.w * xj[3])));
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[s]);  // this warp is done with the stage
+            // Row sums across the 32 lanes by recursive halving (ROWS
+            // shuffles): afterwards lanes G r .. G r + G - 1 hold the sum of
+            // the warp's row r.
+#pragma unroll
+            for (int h = SV_ROWS / 2; h >= 1; h >>= 1) {
+                const int off = SV_G * h;  // 16, 8, 4 (, 2)
+                const bool upper = (lane & off) != 0;
+#pragma unroll
+                for (int q = 0; q < h; ++q) {
+                    const float send = upper ? rp[q] : rp[q + h];
+                    const float keep = upper ? rp[q + h] : rp[q];
+                    rp[q] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+                }
+            }
+#pragma unroll
+            for (int off = SV_G / 2; off >= 1; off >>= 1) rp[0] += __shfl_xor_sync(0xffffffffu, rp[0], off);
+            if ((lane & (SV_G - 1)) == 0)
+                part[(static_cast<int64_t>(bi) * nb + bj) * SV_T + SV_ROWS * warp + lane / SV_G] =
+                    static_cast<double>(rp[0]);
+            // Column sums: the warps' partials through shared memory (two
+            // buffers, so one barrier a tile keeps writers and readers apart).
+            float* rb = red + (k & 1) * SV_CWARPS * SV_T;
+            if (bi != bj) reinterpret_cast<float4*>(rb + warp * SV_T)[lane] = make_float4(cs0, cs1, cs2, cs3);
+            if (consumer_sync_or(!ok, 32 * SV_CWARPS)) break;
+            if (bi != bj && tid < SV_T) {
+                float c = 0.f;
+#pragma unroll
+                for (int w = 0; w < SV_CWARPS; ++w) c += rb[w * SV_T + tid];
+                part[(static_cast<int64_t>(bj) * nb + bi) * SV_T + tid] = static_cast<double>(c);
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) xj[e] = xj_n[e];
+#pragma unroll
+            for (int e = 0; e < SV_ROWS; ++e) xi[e] = xi_n[e];
+        }
+    }
+
+    // ---- teardown: after an abort, let the copies in flight land ----
+    __syncthreads();
+    if (*abort_flag && warp == SV_CWARPS && lane == 0) {
+        for (int g = issued - SV_STAGES; g < issued; ++g) {
+            if (g < 0) continue;
+            if (!mbar_wait_bounded(&full[g % SV_STAGES], static_cast<uint32_t>(g / SV_STAGES) & 1u))
+                atomicCAS(err, 0, DEVERR_DRAIN_WAIT);
+        }
+    }
+}
+
+// y[row] = sum over s = 0..nb-1 of part[(b * nb + s) * 128 + r], row = 128 b + r,
+// in a fixed order: a block of 128 threads covers 32 rows; warp q sums the
+// q-th quarter of the sources for its lane's row, then the quarters are added.
+__global__ void __launch_bounds__(128) lz_symv_reduce_kernel(const double* __restrict__ part, int nb, int64_t n,
+                                                            double* __restrict__ y64, float* __restrict__ y32,
+                                                            const int* skip) {
+    if (skip != nullptr && *skip) return;
+    __shared__ double qs[4][32];
+    const int lane = threadIdx.x % 32, q = threadIdx.x / 32;
+    const int64_t row = static_cast<int64_t>(blockIdx.x) * 32 + lane;
+    const int64_t b = row / SV_T, r = row % SV_T;
+    const int per = (nb + 3) / 4;
+    const int sb = q * per, se = (sb + per < nb) ? sb + per : nb;
+    double acc = 0.0;
+    if (row < n) {
+        const double* p = part + b * nb * SV_T + r;
+        int s = sb;
+        for (; s + 8 <= se; s += 8) {
+            double v[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = p[static_cast<int64_t>(s + e) * SV_T];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) acc += v[e];
+        }
+        for (; s < se; ++s) acc += p[static_cast<int64_t>(s) * SV_T];
+    }
+    qs[q][lane] = acc;
+    __syncthreads();
+    if (q == 0 && row < n) {
+        const double v = ((qs[0][lane] + qs[1][lane]) + qs[2][lane]) + qs[3][lane];
+        if (y64) y64[row] = v;
+        if (y32) y32[row] = static_cast<float>(v);
+    }
+}
+
 // One Lanczos update (single block):
 //   alpha_k = q.w; w -= alpha_k q + beta_old q_old; beta_k = ||w||;
 //   stop tests of src/lanczos.cu:145-159; q_old = q; q = w / beta_k;
@@ -325,8 +555,38 @@ __global__ void lz_trivial_kernel(LzState* st) {
     st->inv_scale = 1.0;
 }
 
+// The tile matvec's operands for one bound: the tensor map of the FP32
+// matrix and the partial-sum buffers.
+struct SymvCtx {
+    bool on = false;
+    CUtensorMap tmap;
+    int nb = 0;
+    double* part = nullptr;
+    int* err = nullptr;
+    int warps = 16;  // consumer warps of the tile kernel
+    int sweeps = 0;  // matvecs launched so far (odd ones walk the tiles backwards)
+};
+
 cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double* y64, float* y32, const int* skip,
-                   int sm_count, cudaStream_t s) {
+                   int sm_count, cudaStream_t s, SymvCtx& sv) {
+    if (sv.on) {
+        const int64_t ntiles = static_cast<int64_t>(sv.nb) * (sv.nb + 1) / 2;
+        const int64_t grid = ntiles < sm_count ? ntiles : sm_count;
+        const int reverse = sv.sweeps++ & 1;
+        if (sv.warps == 8)
+            lz_symv_kernel<8><<<static_cast<unsigned>(grid), 32 * 9, SV_SMEM, s>>>(sv.tmap, n, sv.nb, x, sv.part,
+                                                                                 skip, sv.err, reverse);
+        else
+            lz_symv_kernel<16><<<static_cast<unsigned>(grid), 32 * 17, SV_SMEM, s>>>(sv.tmap, n, sv.nb, x, sv.part,
+                                                                                   skip, sv.err, reverse);
+        count_launch();
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        lz_symv_reduce_kernel<<<static_cast<unsigned>((n + 31) / 32), 128, 0, s>>>(sv.part, sv.nb, n, y64, y32,
+                                                                                  skip);
+        count_launch();
+        return cudaGetLastError();
+    }
     const size_t smem = sizeof(float) * static_cast<size_t>(ld);
     const int threads = 256;
     // At most the CTAs that fit at once (the loop strides over the rest);
@@ -351,7 +611,7 @@ cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double
 
 struct LzPtrs {
     LzState* st;
-    double *alpha, *beta, *q, *w, *vold, *V, *y, *ry, *uk, *work;
+    double *alpha, *beta, *q, *w, *vold, *V, *y, *ry, *uk, *work, *part;
     float *q32, *u32;
 };
 
@@ -372,10 +632,13 @@ LzPtrs lz_ptrs(void* d_state, int64_t n, int64_t m) {
     p.u32 = reinterpret_cast<float*>(base + L.u32);
     p.uk = reinterpret_cast<double*>(base + L.uk);
     p.work = reinterpret_cast<double*>(base + L.work);
+    p.part = reinterpret_cast<double*>(base + L.part);
     return p;
 }
 
 }  // namespace
+
+int g_lanczos_symv = -1;
 
 size_t lanczos_state_bytes(int64_t n, int64_t max_iter) {
     const int64_t m = max_iter < n ? max_iter : n;
@@ -403,8 +666,30 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
         PSDGB_CUDA_TRY(cudaGetLastError());
         return PSDGB_OK;
     }
+    SymvCtx sv;
+    // TMA reads need a 16-byte aligned matrix (a caller's workspace may not be).
+    const bool aligned = (reinterpret_cast<uintptr_t>(a32) & 15u) == 0 && ld % 4 == 0;
+    sv.on = aligned && (g_lanczos_symv >= 1 ? n >= 128 : (g_lanczos_symv < 0 && n >= 2048));
+    if (sv.on) {
+        sv.nb = static_cast<int>((n + SV_T - 1) / SV_T);
+        sv.part = P.part;
+        sv.err = ds->d_error;
+        if (!make_tmap_f32(&sv.tmap, a32, ld, n, n, SV_T, SV_T)) {
+            set_error("Lanczos bound: encoding the tensor map of the FP32 matrix failed");
+            return PSDGB_ERR_CUDA;
+        }
+        sv.warps = g_lanczos_symv == 2 ? 8 : 16;
+        static int smem_set_device = -1;
+        if (smem_set_device != ds->device) {
+            PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_symv_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                static_cast<int>(SV_SMEM)));
+            PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_symv_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                static_cast<int>(SV_SMEM)));
+            smem_set_device = ds->device;
+        }
+    }
     const size_t xs_bytes = sizeof(float) * static_cast<size_t>(ld);
-    if (xs_bytes > 48 * 1024) {
+    if (!sv.on && xs_bytes > 48 * 1024) {
         if (xs_bytes > 200 * 1024) {
             set_error("Lanczos bound: n too large for the shared-memory vector stage (n <= 51200)");
             return PSDGB_ERR_INVALID_ARGUMENT;
@@ -420,8 +705,8 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
 
     const int* stopped = &P.st->stopped;
     for (int64_t k = 0; k < m; ++k) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, ds->sm_count, s));  // u = A q
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s));    // w = A^T u
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, ds->sm_count, s, sv));  // u = A q
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv));    // w = A^T u
         lz_update_kernel<<<1, 1024, 0, s>>>(n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q, P.w, P.vold,
                                             P.V, P.q32);
         count_launch();
@@ -439,10 +724,10 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
     }
     const int* no_ritz = &P.st->no_ritz;
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, no_ritz, ds->sm_count, s));  // A y
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.ry, nullptr, no_ritz, ds->sm_count, s));   // A^T A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, no_ritz, ds->sm_count, s, sv));  // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.ry, nullptr, no_ritz, ds->sm_count, s, sv));   // A^T A y
     } else {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, P.ry, nullptr, no_ritz, ds->sm_count, s));   // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, P.ry, nullptr, no_ritz, ds->sm_count, s, sv));   // A y
     }
     lz_resid_kernel<<<1, 1024, 0, s>>>(n, P.ry, P.y, P.st);
     count_launch();

@@ -162,6 +162,21 @@ def test_deterministic_and_workspace(psd, precision):
     assert np.array_equal(a, c)
 
 
+def test_unaligned_workspace_is_refused(psd):
+    """A caller workspace that is not 16-byte aligned (TMA tensor maps and
+    16-byte vector stores read and write it) gives an invalid-argument error
+    before anything runs; the matrix is untouched."""
+    import torch
+
+    x = gaussian_sym(200, seed=13)
+    ws = torch.empty(psd.workspace_size(200, psd.PRECISIONS["fp16x3"]) + 64, dtype=torch.uint8, device="cuda")
+    t = to_dev(x)
+    with pytest.raises(psd.PsdgbError) as e:
+        psd.composite(t, psd.PRECISIONS["fp16x3"], psd.SCHEDULE_FP32, auto_scale=True, workspace=ws[4:])
+    assert e.value.status == 1 and "aligned" in str(e.value)
+    assert np.array_equal(from_dev(t), x)
+
+
 def test_reference_method_mapping(psd):
     """composite_FP32 / _FP16 / _emulated entry points use fp16x3 / fp16 / bf16x9."""
     x = uniform_spectrum(150, 1.0, seed=12)

@@ -91,3 +91,60 @@ def test_seed_changes_start_but_not_the_bound(psd):
     b = psd.lanczos_details(to_dev(x), 20, 1e-10, seed=2, residual=1)
     assert a["alpha"] != b["alpha"]
     assert a["lo"] == pytest.approx(4.0, rel=1e-3) and b["lo"] == pytest.approx(4.0, rel=1e-3)
+
+
+@pytest.fixture
+def matvec_mode(psd):
+    prev = psd.set_product_tuning(psd.TUNE_LANCZOS_SYMV, -1)
+    yield lambda v: psd.set_product_tuning(psd.TUNE_LANCZOS_SYMV, v)
+    psd.set_product_tuning(psd.TUNE_LANCZOS_SYMV, prev)
+
+
+@pytest.mark.parametrize("n,residual", [(257, 0), (1000, 1), (2048, 0), (2100, 1)])
+def test_triangle_matvec_parity_with_oracle(psd, matvec_mode, n, residual):
+    """The matvec over the lower block triangle (128 x 128 tiles, each giving
+    row and column sums) against the FP64 oracle, with the bars of the
+    whole-matrix matvec."""
+    matvec_mode(1)
+    x = gaussian_sym(n, seed=n + 1)
+    x32 = x.astype(np.float32).astype(np.float64)
+    want = rp.approximate_two_norm(x32, 20, 1e-10, residual=("reference", "exact")[residual])
+    got = psd.lanczos_details(to_dev(x), 20, 1e-10, residual=residual)
+    assert got["nb_iter"] == want["nb_iter"]
+    k = min(want["nb_iter"], 12)
+    np.testing.assert_allclose(got["alpha"][:k], want["alpha"][:k], rtol=2e-5)
+    np.testing.assert_allclose(got["beta"][:k], want["beta"][:k], rtol=2e-4)
+    assert got["lo"] == pytest.approx(want["lo"], rel=1e-6)
+    assert got["up"] == pytest.approx(want["up"], rel=1e-4)
+
+
+@pytest.mark.parametrize("n", [2048, 4100])
+def test_triangle_matvec_matches_column_matvec_and_repeats(psd, matvec_mode, n):
+    """Both matvecs give the same bound; the triangle one is bit-for-bit
+    repeatable (its cross-tile sums run in a fixed order whatever the CTA
+    schedule)."""
+    d = to_dev(gaussian_sym(n, seed=11))
+    matvec_mode(0)
+    col = psd.lanczos_details(d, 20, 1e-10)
+    matvec_mode(1)
+    tri = psd.lanczos_details(d, 20, 1e-10)
+    again = psd.lanczos_details(d, 20, 1e-10)
+    assert tri == again
+    np.testing.assert_allclose(tri["alpha"][:12], col["alpha"][:12], rtol=2e-5)
+    assert tri["lo"] == pytest.approx(col["lo"], rel=1e-6)
+    assert tri["up"] == pytest.approx(col["up"], rel=1e-4)
+
+
+def test_triangle_matvec_large(psd, matvec_mode):
+    """n = 8192 (64 x 64 row blocks): both matvecs agree; with the automatic
+    choice the triangle one runs."""
+    d = to_dev(gaussian_sym(8192, seed=5))
+    out = {}
+    for mode in (0, 1, -1):
+        matvec_mode(mode)
+        out[mode] = psd.lanczos_details(d, 20, 1e-10)
+    assert out[1] == out[-1]
+    np.testing.assert_allclose(out[1]["alpha"][:12], out[0]["alpha"][:12], rtol=2e-5)
+    assert out[1]["lo"] == pytest.approx(out[0]["lo"], rel=1e-6)
+    assert out[1]["up"] == pytest.approx(out[0]["up"], rel=1e-4)
+    assert out[1]["lo"] <= out[1]["up"]
