@@ -49,7 +49,7 @@ struct LzBlockDesc {
     int m;
     int pad;
     long long a32_off;  // floats
-    long long vec_off;  // doubles: V (n*m) | alpha, beta, uk (m+1 each) | work (4(m+1))
+    long long vec_off;  // doubles: V (n*m) | alpha, beta, uk (m+1 each) | work (5(m+1))
     long long x_off;    // doubles into the packed FP64 blocks
 };
 
@@ -212,7 +212,9 @@ __global__ void __launch_bounds__(LZ_THREADS, 2) lz_batch_kernel(const LzBlockDe
         if (threadIdx.x == 0) uk[0] = 1.0;
     } else {
         if (threadIdx.x < 32) {
-            const double t = warp_tridiag_top(alpha, beta, nb, uk, work);
+            // Scratch for the staged T: the q / w / vold vectors (3 ld4 >= 3 nb
+            // doubles of shared memory), unused from here on.
+            const double t = warp_tridiag_top(alpha, beta, nb, uk, work, q);
             if (threadIdx.x == 0) red[0] = t;
         }
         __syncthreads();
@@ -488,7 +490,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         lz[i] = LzBlockDesc{static_cast<int>(n), static_cast<int>(ld4), static_cast<int>(m), 0, aoff, voff, xoff};
         xoff += n * n;
         aoff += up_to(n * ld4, 64);
-        voff += up_to(n * m + 7 * (m + 1), 32);
+        voff += up_to(n * m + 8 * (m + 1), 32);
         max_smem = std::max<size_t>(max_smem, 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float));
     }
     b->total_elems = xoff;

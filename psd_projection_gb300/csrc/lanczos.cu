@@ -51,7 +51,7 @@ struct LzState {
 
 // Layout of the Lanczos state inside its buffer.
 struct LzLayout {
-    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk, work, part;
+    size_t state, alpha, beta, q, w, vold, V, y, ry, q32, u32, uk, work, part, qdot, norm;
     size_t total;
 };
 
@@ -74,9 +74,11 @@ LzLayout lz_layout(int64_t n, int64_t m) {
     L.q32 = take(sizeof(float) * n4);
     L.u32 = take(sizeof(float) * n4);
     L.uk = take(sizeof(double) * (m + 1));
-    L.work = take(sizeof(double) * 4 * (m + 1));  // tridiagonal LU of the inverse iteration
+    L.work = take(sizeof(double) * 8 * (m + 1));  // tridiagonal solver: LU (5 (m+1)) and staged T (3 (m+1))
     const size_t nb = static_cast<size_t>((n + 127) / 128);
     L.part = take(sizeof(double) * nb * nb * 128);  // tile matvec: partial sums [row block][source block][128]
+    L.qdot = take(sizeof(double) * static_cast<size_t>((n + 31) / 32));   // q.w partials (reduce blocks)
+    L.norm = take(sizeof(double) * static_cast<size_t>((n + 511) / 512)); // ||w||^2 partials
     L.total = off;
     return L;
 }
@@ -400,9 +402,12 @@ __global__ void __launch_bounds__(32 * (CW + 1), 1)
 // y[row] = sum over s = 0..nb-1 of part[(b * nb + s) * 128 + r], row = 128 b + r,
 // in a fixed order: a block of 128 threads covers 32 rows; warp q sums the
 // q-th quarter of the sources for its lane's row, then the quarters are added.
+// With qd set, qdot_part[block] = sum over the block's rows of qd[row] y[row]
+// (a fixed shuffle tree): the partials of the Lanczos alpha = q.w.
 __global__ void __launch_bounds__(128) lz_symv_reduce_kernel(const double* __restrict__ part, int nb, int64_t n,
                                                             double* __restrict__ y64, float* __restrict__ y32,
-                                                            const int* skip) {
+                                                            const int* skip, const double* __restrict__ qd,
+                                                            double* __restrict__ qdot_part) {
     if (skip != nullptr && *skip) return;
     __shared__ double qs[4][32];
     const int lane = threadIdx.x % 32, q = threadIdx.x / 32;
@@ -425,25 +430,195 @@ __global__ void __launch_bounds__(128) lz_symv_reduce_kernel(const double* __res
     }
     qs[q][lane] = acc;
     __syncthreads();
-    if (q == 0 && row < n) {
+    if (q == 0) {
         const double v = ((qs[0][lane] + qs[1][lane]) + qs[2][lane]) + qs[3][lane];
-        if (y64) y64[row] = v;
-        if (y32) y32[row] = static_cast<float>(v);
+        if (row < n) {
+            if (y64) y64[row] = v;
+            if (y32) y32[row] = static_cast<float>(v);
+        }
+        if (qd != nullptr) {
+            double p = row < n ? qd[row] * v : 0.0;
+            for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+            if (lane == 0) qdot_part[blockIdx.x] = p;
+        }
     }
 }
 
-// One Lanczos update (single block):
+// ---- the Lanczos update spread over the GPU (with the tile matvec) ----------
+// FP64 issues slowly on this GPU, so the update's vector arithmetic runs in
+// UPB_BLOCKS-wide grids rather than one block.  Every block sums the same
+// partials in the same order, so alpha, beta and the stop test agree.
+constexpr int UPB_THREADS = 256;
+constexpr int UPB_ROWS = 2 * UPB_THREADS;  // rows per block
+
+// Sum of part[0..count) in a fixed order, returned to every thread of the
+// block (red: 32 doubles of shared memory).
+__device__ double sum_parts(const double* __restrict__ part, int count, double* red) {
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < count; i += 32) s += part[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) red[0] = s;
+    }
+    __syncthreads();
+    const double s = red[0];
+    __syncthreads();
+    return s;
+}
+
+// Block-wide FP64 sum in a fixed order, result in thread 0.
+__device__ double block_sum_fixed(double v, double* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < static_cast<int>(blockDim.x / 32); ++i) s += red[i];
+    __syncthreads();
+    return s;
+}
+
+// alpha_k = sum of the q.w partials; w -= alpha_k q + beta_old q_old; the
+// partial sums of ||w||^2 per block.
+__global__ void __launch_bounds__(UPB_THREADS) lz_upd_axpy_kernel(int64_t n, int k, LzState* st, double* alpha,
+                                                                  const double* __restrict__ q, double* w,
+                                                                  const double* __restrict__ vold,
+                                                                  const double* __restrict__ qdot_part, int nqdot,
+                                                                  double* norm_part) {
+    if (st->stopped) return;
+    __shared__ double red[32];
+    const double a = sum_parts(qdot_part, nqdot, red);
+    const double b_old = st->beta_old;
+    double s = 0.0;
+#pragma unroll
+    for (int r = 0; r < UPB_ROWS / UPB_THREADS; ++r) {
+        const int64_t i = static_cast<int64_t>(blockIdx.x) * UPB_ROWS + r * UPB_THREADS + threadIdx.x;
+        if (i < n) {
+            const double v = w[i] - a * q[i] - b_old * vold[i];
+            w[i] = v;
+            s += v * v;
+        }
+    }
+    s = block_sum_fixed(s, red);
+    if (threadIdx.x == 0) {
+        norm_part[blockIdx.x] = s;
+        if (blockIdx.x == 0) alpha[k] = a;
+    }
+}
+
+// beta_k = sqrt(sum of the partials); the stop tests of src/lanczos.cu:145-159;
+// q_old = q; q = w / beta_k; V[:, k+1] = q when k < m-1; nb_iter++.
+__global__ void __launch_bounds__(UPB_THREADS) lz_upd_scale_kernel(int64_t n, int64_t m, int k, double tol,
+                                                                   LzState* st, const double* alpha, double* beta,
+                                                                   double* q, const double* __restrict__ w,
+                                                                   double* vold, double* V, float* q32,
+                                                                   const double* __restrict__ norm_part,
+                                                                   int nnorm) {
+    if (st->stopped) return;
+    __shared__ double red[32];
+    const double b = sqrt(sum_parts(norm_part, nnorm, red));
+    const double a = alpha[k];
+    if (blockIdx.x == 0 && threadIdx.x == 0) beta[k] = b;
+    if ((b <= tol * a && k > 1) || b == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st->stopped = 1;
+        return;
+    }
+    const double inv = 1.0 / b;
+    const bool store_v = (k < m - 1);
+#pragma unroll
+    for (int r = 0; r < UPB_ROWS / UPB_THREADS; ++r) {
+        const int64_t i = static_cast<int64_t>(blockIdx.x) * UPB_ROWS + r * UPB_THREADS + threadIdx.x;
+        if (i < n) {
+            const double qn = w[i] * inv;
+            vold[i] = q[i];
+            q[i] = qn;
+            q32[i] = static_cast<float>(qn);
+            if (store_v) V[static_cast<int64_t>(k + 1) * n + i] = qn;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st->beta_old = b;
+        st->nb_iter = k + 1;
+    }
+}
+
+// One Lanczos update (single block of UPD_THREADS):
 //   alpha_k = q.w; w -= alpha_k q + beta_old q_old; beta_k = ||w||;
 //   stop tests of src/lanczos.cu:145-159; q_old = q; q = w / beta_k;
 //   V[:, k+1] = q when k < m-1; nb_iter++.
-__global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzState* st, double* alpha, double* beta,
-                                 double* q, double* w, double* vold, double* V, float* q32) {
+// For n <= UPD_THREADS * UPD_R each thread loads its UPD_R elements of q, w
+// and q_old once, all up front (one memory latency instead of one per
+// element and pass); the sums run in the same per-thread order either way.
+constexpr int UPD_THREADS = 1024;
+constexpr int UPD_R = 8;
+
+__global__ void __launch_bounds__(UPD_THREADS) lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzState* st,
+                                                                double* alpha, double* beta, double* q, double* w,
+                                                                double* vold, double* V, float* q32) {
     if (st->stopped) return;
     __shared__ double red[32];
+    const double b_old = st->beta_old;
+    const bool store_v = (k < m - 1);
+    double* vnext = V + static_cast<int64_t>(k + 1) * n;
+    if (n <= static_cast<int64_t>(UPD_THREADS) * UPD_R) {
+        double qv[UPD_R], wv[UPD_R], ov[UPD_R];
+#pragma unroll
+        for (int r = 0; r < UPD_R; ++r) {
+            const int64_t i = threadIdx.x + static_cast<int64_t>(r) * UPD_THREADS;
+            const bool in = i < n;
+            qv[r] = in ? q[i] : 0.0;
+            wv[r] = in ? w[i] : 0.0;
+            ov[r] = in ? vold[i] : 0.0;
+        }
+        double s = 0.0;
+#pragma unroll
+        for (int r = 0; r < UPD_R; ++r) s += qv[r] * wv[r];
+        const double a = block_sum(s, red);
+        s = 0.0;
+#pragma unroll
+        for (int r = 0; r < UPD_R; ++r) {
+            wv[r] = wv[r] - a * qv[r] - b_old * ov[r];
+            s += wv[r] * wv[r];
+        }
+        const double b = sqrt(block_sum(s, red));
+        if (threadIdx.x == 0) {
+            alpha[k] = a;
+            beta[k] = b;
+        }
+        if ((b <= tol * a && k > 1) || b == 0.0) {
+#pragma unroll
+            for (int r = 0; r < UPD_R; ++r) {
+                const int64_t i = threadIdx.x + static_cast<int64_t>(r) * UPD_THREADS;
+                if (i < n) w[i] = wv[r];
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) st->stopped = 1;
+            return;
+        }
+        const double inv = 1.0 / b;
+#pragma unroll
+        for (int r = 0; r < UPD_R; ++r) {
+            const int64_t i = threadIdx.x + static_cast<int64_t>(r) * UPD_THREADS;
+            if (i < n) {
+                const double qn = wv[r] * inv;
+                w[i] = wv[r];
+                vold[i] = qv[r];
+                q[i] = qn;
+                q32[i] = static_cast<float>(qn);
+                if (store_v) vnext[i] = qn;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            st->beta_old = b;
+            st->nb_iter = k + 1;
+        }
+        return;
+    }
     double s = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += q[i] * w[i];
     const double a = block_sum(s, red);
-    const double b_old = st->beta_old;
     s = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const double v = w[i] - a * q[i] - b_old * vold[i];
@@ -461,13 +636,12 @@ __global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzStat
         return;
     }
     const double inv = 1.0 / b;
-    const bool store_v = (k < m - 1);
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
         const double qn = w[i] * inv;
         vold[i] = q[i];
         q[i] = qn;
         q32[i] = static_cast<float>(qn);
-        if (store_v) V[static_cast<int64_t>(k + 1) * n + i] = qn;
+        if (store_v) vnext[i] = qn;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -476,8 +650,13 @@ __global__ void lz_update_kernel(int64_t n, int64_t m, int k, double tol, LzStat
     }
 }
 
-// The largest eigenpair of T, by one warp (tridiag.cuh).
-__global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double* beta, double* uk, double* work) {
+// The largest eigenpair of T, by one warp (tridiag.cuh).  The solver's
+// 8 (mx) doubles of work and scratch live in dynamic shared memory when the
+// launch provides it (smem != 0), else in `work` (global, 8 mx doubles);
+// mx = max_iter + 1 >= nb_iter.
+__global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double* beta, double* uk, double* work,
+                                  int64_t mx, int smem) {
+    extern __shared__ double tsm[];
     const int lane = threadIdx.x;
     const int64_t m = st->nb_iter;
     if (m == 0) {  // the all-zero branch of src/lanczos.cu:171-184
@@ -499,7 +678,8 @@ __global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double
         }
         return;
     }
-    const double t = warp_tridiag_top(alpha, beta, m, uk, work);
+    double* base = smem ? tsm : work;
+    const double t = warp_tridiag_top(alpha, beta, m, uk, base, base + 5 * mx);
     if (lane == 0) {
         st->no_ritz = 0;
         st->theta = t;
@@ -568,7 +748,8 @@ struct SymvCtx {
 };
 
 cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double* y64, float* y32, const int* skip,
-                   int sm_count, cudaStream_t s, SymvCtx& sv) {
+                   int sm_count, cudaStream_t s, SymvCtx& sv, const double* qd = nullptr,
+                   double* qdot_part = nullptr) {
     if (sv.on) {
         const int64_t ntiles = static_cast<int64_t>(sv.nb) * (sv.nb + 1) / 2;
         const int64_t grid = ntiles < sm_count ? ntiles : sm_count;
@@ -583,7 +764,7 @@ cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         lz_symv_reduce_kernel<<<static_cast<unsigned>((n + 31) / 32), 128, 0, s>>>(sv.part, sv.nb, n, y64, y32,
-                                                                                  skip);
+                                                                                  skip, qd, qdot_part);
         count_launch();
         return cudaGetLastError();
     }
@@ -611,7 +792,7 @@ cudaError_t matvec(const float* A, int64_t n, int64_t ld, const float* x, double
 
 struct LzPtrs {
     LzState* st;
-    double *alpha, *beta, *q, *w, *vold, *V, *y, *ry, *uk, *work, *part;
+    double *alpha, *beta, *q, *w, *vold, *V, *y, *ry, *uk, *work, *part, *qdot, *norm;
     float *q32, *u32;
 };
 
@@ -633,6 +814,8 @@ LzPtrs lz_ptrs(void* d_state, int64_t n, int64_t m) {
     p.uk = reinterpret_cast<double*>(base + L.uk);
     p.work = reinterpret_cast<double*>(base + L.work);
     p.part = reinterpret_cast<double*>(base + L.part);
+    p.qdot = reinterpret_cast<double*>(base + L.qdot);
+    p.norm = reinterpret_cast<double*>(base + L.norm);
     return p;
 }
 
@@ -704,15 +887,34 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
     PSDGB_CUDA_TRY(cudaGetLastError());
 
     const int* stopped = &P.st->stopped;
+    const int nqdot = static_cast<int>((n + 31) / 32);
+    const int nnorm = static_cast<int>((n + UPB_ROWS - 1) / UPB_ROWS);
     for (int64_t k = 0; k < m; ++k) {
         PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, ds->sm_count, s, sv));  // u = A q
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv));    // w = A^T u
-        lz_update_kernel<<<1, 1024, 0, s>>>(n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q, P.w, P.vold,
-                                            P.V, P.q32);
-        count_launch();
-        PSDGB_CUDA_TRY(cudaGetLastError());
+        if (sv.on) {
+            // w = A^T u with the q.w partials; the update over nnorm blocks.
+            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv, P.q, P.qdot));
+            lz_upd_axpy_kernel<<<static_cast<unsigned>(nnorm), UPB_THREADS, 0, s>>>(
+                n, static_cast<int>(k), P.st, P.alpha, P.q, P.w, P.vold, P.qdot, nqdot, P.norm);
+            count_launch();
+            PSDGB_CUDA_TRY(cudaGetLastError());
+            lz_upd_scale_kernel<<<static_cast<unsigned>(nnorm), UPB_THREADS, 0, s>>>(
+                n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q, P.w, P.vold, P.V, P.q32, P.norm, nnorm);
+            count_launch();
+            PSDGB_CUDA_TRY(cudaGetLastError());
+        } else {
+            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv));  // w = A^T u
+            lz_update_kernel<<<1, UPD_THREADS, 0, s>>>(n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q,
+                                                       P.w, P.vold, P.V, P.q32);
+            count_launch();
+            PSDGB_CUDA_TRY(cudaGetLastError());
+        }
     }
-    lz_tridiag_kernel<<<1, 32, 0, s>>>(P.st, P.alpha, P.beta, P.uk, P.work);
+    {
+        const size_t tsmem = sizeof(double) * 8 * static_cast<size_t>(m + 1);
+        const int use_smem = tsmem <= 48 * 1024 ? 1 : 0;
+        lz_tridiag_kernel<<<1, 32, use_smem ? tsmem : 0, s>>>(P.st, P.alpha, P.beta, P.uk, P.work, m + 1, use_smem);
+    }
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     {
