@@ -9,7 +9,9 @@
 //   batch_to_f32      every block's upper triangle -> FP32 symmetric copy
 //   lz_batch_kernel   one CTA per block runs the whole Lanczos bound of its
 //                     block (recurrence, tridiagonal eigenpair, Ritz residual)
-//                     and leaves the block's scale 1/up on the device
+//                     and leaves the block's scale 1/up on the device; one
+//                     launch per size class (64 / 128 / 256 / 512 threads by
+//                     n), so small blocks run many CTAs per SM
 //   batch_split       scaled operand terms into one strided layout
 //   3 x steps         grouped persistent tensor-core products over the tile
 //                     list of all blocks (gemm_tc.cu)
@@ -34,7 +36,12 @@ namespace {
 
 using namespace psdgb;
 
-constexpr int LZ_THREADS = 512;   // Lanczos: one CTA per block
+constexpr int LZ_CLASSES = 4;     // Lanczos CTA sizes 512, 256, 128, 64 threads
+constexpr int kLzThreads[LZ_CLASSES] = {512, 256, 128, 64};
+
+// Lanczos CTA size class of a block of size n: the smallest CTA of at least
+// n threads, between 64 and 512.
+inline int lz_class(int64_t n) { return n > 256 ? 0 : (n > 128 ? 1 : (n > 64 ? 2 : 3)); }
 constexpr int COPY_THREADS = 256;  // 32 x 8 transpose tiles
 constexpr int COPY_SPLIT = 16;     // CTAs per block for the copy / split kernels
 
@@ -119,17 +126,72 @@ __device__ void cta_matvec(const float* __restrict__ A, int n, int ld4, const fl
     }
 }
 
-// The Lanczos bound of one block per CTA (src/lanczos.cu:41-293, as in lanczos.cu).
-__global__ void __launch_bounds__(LZ_THREADS, 2) lz_batch_kernel(const LzBlockDesc* __restrict__ descs,
+// y[c] = sum_r A[c*ld4 + r] x[r] with one column per thread (blocks of at
+// most 128 in CTAs of 64 or 128 threads): each thread streams its own
+// column with eight 16-byte loads in flight and sums it in FP32, one FP64
+// conversion per column; no cross-lane reduction, so a matvec costs a few
+// memory round trips instead of one per group of four columns.
+__device__ void cta_matvec_cols(const float* __restrict__ A, int n, int ld4, const float* xs, double* y64,
+                                float* y32) {
+    const float4* xs4 = reinterpret_cast<const float4*>(xs);
+    const int kv = ld4 / 4;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        const float4* col = reinterpret_cast<const float4*>(A + static_cast<int64_t>(c) * ld4);
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+        int k = 0;
+        for (; k + 8 <= kv; k += 8) {
+            float4 a[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) a[j] = __ldg(col + k + j);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const float4 xb = xs4[k + j];
+                s0 = fmaf(a[j].x, xb.x, s0);
+                s1 = fmaf(a[j].y, xb.y, s1);
+                s2 = fmaf(a[j].z, xb.z, s2);
+                s3 = fmaf(a[j].w, xb.w, s3);
+            }
+        }
+        for (; k < kv; ++k) {
+            const float4 a = __ldg(col + k);
+            const float4 xb = xs4[k];
+            s0 = fmaf(a.x, xb.x, s0);
+            s1 = fmaf(a.y, xb.y, s1);
+            s2 = fmaf(a.z, xb.z, s2);
+            s3 = fmaf(a.w, xb.w, s3);
+        }
+        const float acc = (s0 + s1) + (s2 + s3);
+        if (y64) y64[c] = static_cast<double>(acc);
+        if (y32) y32[c] = acc;
+    }
+}
+
+// The matvec of a T-thread Lanczos CTA.
+template <int T>
+__device__ __forceinline__ void lz_matvec(const float* __restrict__ A, int n, int ld4, const float* xs, double* y64,
+                                          float* y32) {
+    if (T <= 128)
+        cta_matvec_cols(A, n, ld4, xs, y64, y32);
+    else
+        cta_matvec(A, n, ld4, xs, y64, y32);
+}
+
+// The Lanczos bound of one block per CTA (src/lanczos.cu:41-293, as in
+// lanczos.cu): CTA blockIdx.x takes block idx[blockIdx.x].  T threads, at
+// most 64 registers each (1024 / T CTAs per SM by registers).
+template <int T>
+__global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc* __restrict__ descs,
+                                                              const int* __restrict__ idx,
                                                               const float* __restrict__ a32, double* vec,
                                                               BatchState* states, double tol, uint64_t seed,
                                                               int residual_mode) {
     extern __shared__ double sh[];
     __shared__ double red[32];
-    __shared__ double part[LZ_THREADS];
-    const LzBlockDesc d = descs[blockIdx.x];
+    __shared__ double part[T];
+    const int bidx = idx[blockIdx.x];
+    const LzBlockDesc d = descs[bidx];
     const int n = d.n, ld4 = d.ld4, m = d.m;
-    BatchState* st = states + blockIdx.x;
+    BatchState* st = states + bidx;
     if (m <= 0) {
         if (threadIdx.x == 0) *st = BatchState{0.0, 0.0, 1.0, 1.0, 1.0, 0, 0};
         return;
@@ -171,9 +233,9 @@ __global__ void __launch_bounds__(LZ_THREADS, 2) lz_batch_kernel(const LzBlockDe
     int nb = 0;
     for (int k = 0; k < m; ++k) {
         __syncthreads();
-        cta_matvec(A, n, ld4, x32, nullptr, u32);  // u = A q
+        lz_matvec<T>(A, n, ld4, x32, nullptr, u32);  // u = A q
         __syncthreads();
-        cta_matvec(A, n, ld4, u32, w, nullptr);    // w = A^T u
+        lz_matvec<T>(A, n, ld4, u32, w, nullptr);    // w = A^T u
         __syncthreads();
         double s = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) s += q[i] * w[i];
@@ -230,11 +292,11 @@ __global__ void __launch_bounds__(LZ_THREADS, 2) lz_batch_kernel(const LzBlockDe
     }
     __syncthreads();
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
-        cta_matvec(A, n, ld4, x32, nullptr, u32);
+        lz_matvec<T>(A, n, ld4, x32, nullptr, u32);
         __syncthreads();
-        cta_matvec(A, n, ld4, u32, ry, nullptr);
+        lz_matvec<T>(A, n, ld4, u32, ry, nullptr);
     } else {
-        cta_matvec(A, n, ld4, x32, ry, nullptr);
+        lz_matvec<T>(A, n, ld4, x32, ry, nullptr);
     }
     __syncthreads();
     double s = 0.0;
@@ -285,42 +347,72 @@ __global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const
 // Operand terms of block b into the strided layout: from the FP32 copy
 // (from_x == 0) or the FP64 input (from_x != 0, upper triangle), times the
 // block's 1/up; zero in the padding of the block's np x np region.
-__global__ void batch_split_kernel(const LzBlockDesc* __restrict__ lz, const BlockDesc* __restrict__ blocks,
-                                   const BatchState* __restrict__ states, const float* __restrict__ a32,
-                                   const double* __restrict__ x, int from_x, SplitMat out, int fmt, int64_t ld) {
-    __shared__ double sm[32][33];
+// Scaled operand terms of every block into the strided layout: from the
+// FP32 copy (from_x = 0, the first split) or from the caller's FP64 blocks
+// (from_x = 1, Xs = X / up).  The CTA walks pairs of 32 x 32 tiles of its
+// block's np x np area (zero outside n), one tile per half; each thread
+// writes 8 consecutive elements as one 16-byte store per term plane.
+__global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlockDesc* __restrict__ lz,
+                                                                   const BlockDesc* __restrict__ blocks,
+                                                                   const BatchState* __restrict__ states,
+                                                                   const float* __restrict__ a32,
+                                                                   const double* __restrict__ x, int from_x,
+                                                                   SplitMat out, int fmt, int64_t ld) {
+    static_assert(COPY_THREADS == 256, "two halves of 128 threads");
+    __shared__ double sm[2][32][33];
     const LzBlockDesc d = lz[blockIdx.x];
     const BlockDesc bd = blocks[blockIdx.x];
     const double inv = states[blockIdx.x].inv_scale;
     const int n = d.n, np = bd.np;
-    const int tx = threadIdx.x % 32, ty0 = threadIdx.x / 32;
+    const int h = threadIdx.x / 128, ht = threadIdx.x % 128;
+    const int tx = ht % 32, ty0 = ht / 32;        // load phase: 32 x 4
+    const int r = ht / 4, g = ht % 4;             // store phase: row r, columns 8g..8g+7
     const int nt = np / 32;
+    const int ntiles = nt * nt;
     const double* X = x + d.x_off;
     const float* A = a32 + d.a32_off;
-    for (int t = blockIdx.y; t < nt * nt; t += gridDim.y) {
-        const int bi = t / nt, bj = t % nt;
+    const bool vec_ok = (d.ld4 % 4) == 0;
+    for (int tp = blockIdx.y; 2 * tp < ntiles; tp += gridDim.y) {
+        const int t = 2 * tp + h;
+        const bool valid = t < ntiles;
+        const int bi = valid ? t / nt : 0, bj = valid ? t % nt : 0;
         if (from_x) {
             const int rbase = (bi <= bj) ? bi * 32 : bj * 32;
             const int cbase = (bi <= bj) ? bj * 32 : bi * 32;
             __syncthreads();
-            for (int ty = ty0; ty < 32; ty += 8) {
-                const int r = rbase + tx, c = cbase + ty;
-                sm[ty][tx] = (r < n && c < n) ? X[r + static_cast<int64_t>(c) * n] : 0.0;
+            for (int ty = ty0; ty < 32; ty += 4) {
+                const int rr = rbase + tx, c = cbase + ty;
+                sm[h][ty][tx] = (valid && rr < n && c < n) ? X[rr + static_cast<int64_t>(c) * n] : 0.0;
             }
             __syncthreads();
         }
-        for (int ty = ty0; ty < 32; ty += 8) {
-            const int i = bi * 32 + ty, j = bj * 32 + tx;
-            double v = 0.0;
-            if (i < n && j < n) {
-                if (from_x)
-                    v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
-                else
-                    v = A[static_cast<int64_t>(i) * d.ld4 + j];
+        if (!valid) continue;
+        const int i = bi * 32 + r, j0 = bj * 32 + 8 * g;
+        float v[8];
+        if (from_x) {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const int cl = 8 * g + e;
+                double val = 0.0;
+                if (i < n && j0 + e < n)
+                    val = (bi < bj) ? sm[h][cl][r] : (bi > bj) ? sm[h][r][cl] : ((r <= cl) ? sm[h][cl][r] : sm[h][r][cl]);
+                v[e] = static_cast<float>(val * inv);
             }
-            split_store(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j,
-                        static_cast<float>(v * inv));
+        } else if (vec_ok && i < n && j0 + 8 <= n) {
+            const float* src = A + static_cast<int64_t>(i) * d.ld4 + j0;
+            const float4 u0 = *reinterpret_cast<const float4*>(src);
+            const float4 u1 = *reinterpret_cast<const float4*>(src + 4);
+            const float w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+            for (int e = 0; e < 8; ++e) v[e] = static_cast<float>(static_cast<double>(w[e]) * inv);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                const double val = (i < n && j0 + e < n) ? A[static_cast<int64_t>(i) * d.ld4 + j0 + e] : 0.0;
+                v[e] = static_cast<float>(val * inv);
+            }
         }
+        split_store8(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j0, v);
     }
 }
 
@@ -344,7 +436,9 @@ struct psdgb_batch {
     double* vec = nullptr;
     SplitMat A{}, A2{}, A3{};
     int64_t num_tiles = 0;
-    size_t lz_smem = 0;
+    int* lz_idx = nullptr;              // block indices grouped by Lanczos size class
+    int64_t lz_start[LZ_CLASSES + 1] = {0, 0, 0, 0, 0};
+    size_t lz_smem[LZ_CLASSES] = {0, 0, 0, 0};
     // tuning
     int acc_mode = ACC_1X4;
     int order = 0;
@@ -360,10 +454,25 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     batch_to_f32_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, d_blocks, b->a32);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
-    lz_batch_kernel<<<count, LZ_THREADS, b->lz_smem, s>>>(b->lz, b->a32, b->vec, b->states, b->tol, b->seed,
-                                                        PSDGB_RESIDUAL_REFERENCE);
-    count_launch();
-    PSDGB_CUDA_TRY(cudaGetLastError());
+    for (int c = 0; c < LZ_CLASSES; ++c) {
+        const int64_t cnt = b->lz_start[c + 1] - b->lz_start[c];
+        if (cnt == 0) continue;
+        const int* idx = b->lz_idx + b->lz_start[c];
+        const unsigned g = static_cast<unsigned>(cnt);
+        const size_t sm = b->lz_smem[c];
+        switch (c) {
+            case 0: lz_batch_kernel<512><<<g, 512, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+                                                            PSDGB_RESIDUAL_REFERENCE); break;
+            case 1: lz_batch_kernel<256><<<g, 256, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+                                                            PSDGB_RESIDUAL_REFERENCE); break;
+            case 2: lz_batch_kernel<128><<<g, 128, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+                                                            PSDGB_RESIDUAL_REFERENCE); break;
+            default: lz_batch_kernel<64><<<g, 64, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+                                                           PSDGB_RESIDUAL_REFERENCE); break;
+        }
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
+    }
     batch_split_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 0, b->A,
                                                          b->fmt, b->ld);
     count_launch();
@@ -482,7 +591,6 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     }
     b->rows = row + shelf_h;
     int64_t xoff = 0, aoff = 0, voff = 0;
-    size_t max_smem = 0;
     for (int64_t i = 0; i < count; ++i) {
         const int64_t n = b->n[i], ld4 = up_to(std::max<int64_t>(n, 1), 4);
         const int64_t m = std::min<int64_t>(b->max_iter, n);
@@ -491,10 +599,19 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         xoff += n * n;
         aoff += up_to(n * ld4, 64);
         voff += up_to(n * m + 8 * (m + 1), 32);
-        max_smem = std::max<size_t>(max_smem, 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float));
+        const int c = lz_class(n);
+        b->lz_smem[c] = std::max<size_t>(b->lz_smem[c], 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float));
     }
     b->total_elems = xoff;
-    b->lz_smem = max_smem;
+    // Lanczos launch order: blocks grouped by size class, largest class first.
+    std::vector<int> lz_order;
+    lz_order.reserve(count);
+    for (int c = 0; c < LZ_CLASSES; ++c) {
+        b->lz_start[c] = static_cast<int64_t>(lz_order.size());
+        for (int64_t i = 0; i < count; ++i)
+            if (lz_class(b->n[i]) == c) lz_order.push_back(static_cast<int>(i));
+    }
+    b->lz_start[LZ_CLASSES] = static_cast<int64_t>(lz_order.size());
     // Tile lists: LPT (largest K first) and block order.
     std::vector<TileDesc> tl_block;
     for (int64_t i = 0; i < count; ++i) {
@@ -514,10 +631,11 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_lz = a256(sizeof(LzBlockDesc) * std::max<int64_t>(count, 1));
     const size_t sz_tiles = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles, 1));
     const size_t sz_states = a256(sizeof(BatchState) * std::max<int64_t>(count, 1));
+    const size_t sz_idx = a256(sizeof(int) * std::max<int64_t>(count, 1));
     const size_t sz_a32 = a256(sizeof(float) * std::max<int64_t>(aoff, 1));
     const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
     const size_t sz_ops = 3 * nterms * a256(plane);
-    b->dev_bytes = sz_blocks + sz_lz + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_ops;
+    b->dev_bytes = sz_blocks + sz_lz + sz_idx + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_ops;
     cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -530,6 +648,8 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     p += sz_blocks;
     b->lz = reinterpret_cast<LzBlockDesc*>(p);
     p += sz_lz;
+    b->lz_idx = reinterpret_cast<int*>(p);
+    p += sz_idx;
     b->tiles[0] = reinterpret_cast<TileDesc*>(p);
     p += sz_tiles;
     b->tiles[1] = reinterpret_cast<TileDesc*>(p);
@@ -550,6 +670,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     if (count > 0) {
         PSDGB_CUDA_TRY(cudaMemcpy(b->blocks, bd.data(), sizeof(BlockDesc) * count, cudaMemcpyHostToDevice));
         PSDGB_CUDA_TRY(cudaMemcpy(b->lz, lz.data(), sizeof(LzBlockDesc) * count, cudaMemcpyHostToDevice));
+        PSDGB_CUDA_TRY(cudaMemcpy(b->lz_idx, lz_order.data(), sizeof(int) * count, cudaMemcpyHostToDevice));
     }
     if (b->num_tiles > 0) {
         PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[0], tl_lpt.data(), sizeof(TileDesc) * b->num_tiles,
@@ -560,9 +681,11 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     // Padding rows/columns between blocks are never read; zero the planes once
     // so every TMA box reads finite values.
     PSDGB_CUDA_TRY(cudaMemset(b->A.term[0], 0, sz_ops));
-    if (b->lz_smem > 48 * 1024)
-        PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            static_cast<int>(b->lz_smem)));
+    // Only the 512-thread class holds blocks large enough (n > 256) to need
+    // more than 48 KB of dynamic shared memory.
+    if (b->lz_smem[0] > 48 * 1024)
+        PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_batch_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            static_cast<int>(b->lz_smem[0])));
     *out = b;
     return PSDGB_OK;
 }

@@ -65,6 +65,42 @@ __device__ __forceinline__ void split_store(const SplitMat& m, int fmt, size_t i
     static_cast<__nv_bfloat16*>(m.term[2])[idx] = b2;
 }
 
+// split_store for 8 consecutive elements (idx a multiple of 8): the same
+// arithmetic, one 16-byte store per term plane.
+__device__ __forceinline__ void split_store8(const SplitMat& m, int fmt, size_t idx, const float (&v)[8]) {
+    if (fmt == FMT_F32) {
+        float4* d = reinterpret_cast<float4*>(static_cast<float*>(m.term[0]) + idx);
+        d[0] = make_float4(v[0], v[1], v[2], v[3]);
+        d[1] = make_float4(v[4], v[5], v[6], v[7]);
+        return;
+    }
+    if (fmt == FMT_F16) {
+        __align__(16) __half h[8];
+        __align__(16) __half l[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            h[e] = __float2half_rn(v[e]);
+            l[e] = __float2half_rn(v[e] - __half2float(h[e]));
+        }
+        *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[0]) + idx) = *reinterpret_cast<const uint4*>(h);
+        *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[1]) + idx) = *reinterpret_cast<const uint4*>(l);
+        return;
+    }
+    __align__(16) __nv_bfloat16 b0[8];
+    __align__(16) __nv_bfloat16 b1[8];
+    __align__(16) __nv_bfloat16 b2[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+        b0[e] = __float2bfloat16_rn(v[e]);
+        const float r1 = v[e] - __bfloat162float(b0[e]);
+        b1[e] = __float2bfloat16_rn(r1);
+        b2[e] = __float2bfloat16_rn(r1 - __bfloat162float(b1[e]));
+    }
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[0]) + idx) = *reinterpret_cast<const uint4*>(b0);
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[1]) + idx) = *reinterpret_cast<const uint4*>(b1);
+    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(m.term[2]) + idx) = *reinterpret_cast<const uint4*>(b2);
+}
+
 #endif  // __CUDACC__
 
 // ---------------------------------------------------------------------------
