@@ -273,14 +273,9 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
         theta = alpha[0];
         if (threadIdx.x == 0) uk[0] = 1.0;
     } else {
-        if (threadIdx.x < 32) {
-            // Scratch for the staged T: the q / w / vold vectors (3 ld4 >= 3 nb
-            // doubles of shared memory), unused from here on.
-            const double t = warp_tridiag_top(alpha, beta, nb, uk, work, q);
-            if (threadIdx.x == 0) red[0] = t;
-        }
-        __syncthreads();
-        theta = red[0];
+        // Scratch for the staged T: the q / w / vold vectors (3 ld4 >= 3 nb
+        // doubles of shared memory), unused from here on.
+        theta = block_tridiag_top(alpha, beta, nb, uk, work, q);
     }
     __syncthreads();
     // Ritz vector y = V u and the residual

@@ -650,14 +650,14 @@ __global__ void __launch_bounds__(UPD_THREADS) lz_update_kernel(int64_t n, int64
     }
 }
 
-// The largest eigenpair of T, by one warp (tridiag.cuh).  The solver's
+// The largest eigenpair of T, by one block of 128 threads (tridiag.cuh).  The solver's
 // 8 (mx) doubles of work and scratch live in dynamic shared memory when the
 // launch provides it (smem != 0), else in `work` (global, 8 mx doubles);
 // mx = max_iter + 1 >= nb_iter.
 __global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double* beta, double* uk, double* work,
                                   int64_t mx, int smem) {
     extern __shared__ double tsm[];
-    const int lane = threadIdx.x;
+    const int lane = threadIdx.x;  // thread index in the block
     const int64_t m = st->nb_iter;
     if (m == 0) {  // the all-zero branch of src/lanczos.cu:171-184
         if (lane == 0) {
@@ -679,7 +679,7 @@ __global__ void lz_tridiag_kernel(LzState* st, const double* alpha, const double
         return;
     }
     double* base = smem ? tsm : work;
-    const double t = warp_tridiag_top(alpha, beta, m, uk, base, base + 5 * mx);
+    const double t = block_tridiag_top(alpha, beta, m, uk, base, base + 5 * mx);
     if (lane == 0) {
         st->no_ritz = 0;
         st->theta = t;
@@ -913,7 +913,7 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
     {
         const size_t tsmem = sizeof(double) * 8 * static_cast<size_t>(m + 1);
         const int use_smem = tsmem <= 48 * 1024 ? 1 : 0;
-        lz_tridiag_kernel<<<1, 32, use_smem ? tsmem : 0, s>>>(P.st, P.alpha, P.beta, P.uk, P.work, m + 1, use_smem);
+        lz_tridiag_kernel<<<1, 128, use_smem ? tsmem : 0, s>>>(P.st, P.alpha, P.beta, P.uk, P.work, m + 1, use_smem);
     }
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());

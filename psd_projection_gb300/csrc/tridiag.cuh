@@ -3,41 +3,30 @@
 //
 // The reference forms the Lanczos tridiagonal T densely and takes the last
 // eigenpair of cuSOLVER Dsyevd (src/lanczos.cu:186-240).  Here one warp:
-// theta by 129-way multisection on the Sturm count (each lane evaluates four
-// split points as interleaved recurrences, a ballot picks the sub-interval;
-// about 8 rounds to full FP64 precision), then the eigenvector by inverse
-// iteration in lane 0 (one factorisation, four solves).  Divisions are
-// reciprocal multiplies (__drcp_rn): FP64 arithmetic issues slowly on this
-// part and these loops are latency-bound, so T is first staged in the
-// caller's scratch (shared memory) with e^2 precomputed.
+// theta by multisection on the Sturm count over up to four warps (129 split
+// points a round, about 8 rounds to full FP64 precision), then the
+// eigenvector by inverse iteration in thread 0 (one factorisation, two
+// solves).  Divisions are reciprocal multiplies (__drcp_rn), and T is first
+// staged in the caller's scratch (shared memory) with e^2 precomputed.
 #pragma once
 
 #include "common.cuh"
 
 namespace psdgb {
 
-// Sturm counts of four shifts at once: cnt[j] = number of eigenvalues of T
-// strictly less than x[j] (signs of the LDL^T pivots of T - x[j] I).  The four
-// recurrences are independent and interleaved, which hides the latency of the
-// FP64 reciprocals; e2[i] = e[i]^2.
-__device__ inline void sturm_count4(const double* d, const double* e2, int64_t m, const double (&x)[4],
-                                    double pivmin, int (&cnt)[4]) {
-    double q[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        q[j] = d[0] - x[j];
-        if (fabs(q[j]) < pivmin) q[j] = -pivmin;
-        cnt[j] = q[j] < 0 ? 1 : 0;
-    }
+// Number of eigenvalues of T strictly less than x (signs of the LDL^T
+// pivots of T - x I); e2[i] = e[i]^2.
+__device__ inline int sturm_count(const double* d, const double* e2, int64_t m, double x, double pivmin) {
+    int cnt = 0;
+    double q = d[0] - x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    if (q < 0) ++cnt;
     for (int64_t i = 1; i < m; ++i) {
-        const double di = d[i], ei = e2[i - 1];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            q[j] = di - x[j] - ei * __drcp_rn(q[j]);
-            if (fabs(q[j]) < pivmin) q[j] = -pivmin;
-            cnt[j] += q[j] < 0 ? 1 : 0;
-        }
+        q = d[i] - x - e2[i - 1] * __drcp_rn(q);
+        if (fabs(q) < pivmin) q = -pivmin;
+        if (q < 0) ++cnt;
     }
+    return cnt;
 }
 
 // LU factorisation with partial pivoting of the band of T - shift I (fill-in
@@ -106,23 +95,35 @@ __device__ inline void tridiag_apply(int64_t m, const double* work, double* b) {
     for (int64_t i = m - 3; i >= 0; --i) b[i] = (b[i] - du[i] * b[i + 1] - du2[i] * b[i + 2]) * rdd[i];
 }
 
-// Whole warp: largest eigenvalue theta of T (diag d[0..m), off-diagonal
-// e[0..m-1)), m >= 2, and a unit eigenvector in u (lane 0 writes u; every
-// lane returns theta).  scratch holds 3m doubles (d, e, e^2 are staged there;
-// shared memory where the caller has it), work 5m.
-__device__ inline double warp_tridiag_top(const double* d_in, const double* e_in, int64_t m, double* u, double* work,
-                                          double* scratch) {
-    const int lane = threadIdx.x & 31;
+// Whole block (every thread calls it; it synchronises the block): the
+// largest eigenvalue theta of T (diag d[0..m), off-diagonal e[0..m-1)),
+// m >= 2, returned to every thread, and a unit eigenvector in u (written by
+// thread 0; synchronise before reading it).  scratch holds 3m doubles (T is
+// staged there with e^2; shared memory where the caller has it), work 5m.
+//
+// An FP64 warp instruction occupies its scheduler for many cycles on this
+// GPU whatever the number of active lanes, so the cost is the count of
+// dependent FP64 warp instructions: each round, W = min(4, warps) warps (one
+// per scheduler) evaluate one Sturm chain per lane, splitting [lo, hi) at
+// 32 W points, and the first split point with every eigenvalue below it is
+// found from the warps' ballots.  Every thread computes the split points
+// with the same formula, so lo and hi are the same numbers everywhere.
+__device__ inline double block_tridiag_top(const double* d_in, const double* e_in, int64_t m, double* u,
+                                           double* work, double* scratch) {
+    __shared__ unsigned masks[2][4];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int W = min(4, static_cast<int>(blockDim.x >> 5));
+    const int P = 32 * W;
     double* d = scratch;
     double* e = scratch + m;
     double* e2 = scratch + 2 * m;
-    for (int64_t i = lane; i < m; i += 32) {
+    for (int64_t i = tid; i < m; i += blockDim.x) {
         d[i] = d_in[i];
         const double ei = (i + 1 < m) ? e_in[i] : 0.0;
         e[i] = ei;
         e2[i] = ei * ei;
     }
-    __syncwarp();
+    __syncthreads();
     double lo = INFINITY, hi = -INFINITY, tnorm = 0.0;
     for (int64_t i = 0; i < m; ++i) {
         const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i + 1 < m ? fabs(e[i]) : 0.0);
@@ -135,47 +136,42 @@ __device__ inline double warp_tridiag_top(const double* d_in, const double* e_in
     const double pad = 2.0 * eps * tnorm + pivmin;
     lo -= pad;
     hi += pad;
-    // Invariant: count(lo) < m <= count(hi); the largest eigenvalue lies in
-    // [lo, hi).  Each round splits [lo, hi) at 128 points (four per lane);
-    // every lane computes the split points with the same formula, so the new
-    // ends are the same numbers in every lane.
-    constexpr double kStep = 1.0 / 129.0;
+    // Invariant: count(lo) < m <= count(hi); the largest eigenvalue lies in [lo, hi).
+    const double step = 1.0 / static_cast<double>(P + 1);
     for (int it = 0; it < 64; ++it) {
         if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
         const double w = hi - lo;
-        double x[4];
-        int cnt[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) x[j] = lo + w * (static_cast<double>(4 * lane + j + 1) * kStep);
-        sturm_count4(d, e2, m, x, pivmin, cnt);
-        int first_local = 4;
-#pragma unroll
-        for (int j = 3; j >= 0; --j) {
-            const bool above = (x[j] > lo && x[j] < hi) ? (cnt[j] >= m) : (x[j] >= hi);
-            if (above) first_local = j;
+        bool above = false;
+        if (warp < W) {
+            const double x = lo + w * (static_cast<double>(warp * 32 + lane + 1) * step);
+            above = (x > lo && x < hi) ? (sturm_count(d, e2, m, x, pivmin) >= m) : (x >= hi);
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, first_local < 4);
-        int g;  // first split point (0..127) with every eigenvalue below it, 128 if none
-        if (mask) {
-            const int L = __ffs(mask) - 1;
-            g = 4 * L + __shfl_sync(0xffffffffu, first_local, L);
-        } else {
-            g = 128;
+        const unsigned ballot = __ballot_sync(0xffffffffu, above);
+        if (warp < W && lane == 0) masks[it & 1][warp] = ballot;
+        __syncthreads();
+        int g = P;  // first split point with every eigenvalue below it, P if none
+        for (int ww = 0; ww < W; ++ww) {
+            const unsigned b = masks[it & 1][ww];
+            if (b) {
+                g = 32 * ww + __ffs(b) - 1;
+                break;
+            }
         }
-        const double new_hi = (g < 128) ? lo + w * (static_cast<double>(g + 1) * kStep) : hi;
-        const double new_lo = (g > 0) ? lo + w * (static_cast<double>(g) * kStep) : lo;
+        const double new_hi = (g < P) ? lo + w * (static_cast<double>(g + 1) * step) : hi;
+        const double new_lo = (g > 0) ? lo + w * (static_cast<double>(g) * step) : lo;
         if (!(new_hi < hi || new_lo > lo)) break;  // no progress at this precision
         hi = new_hi;
         lo = new_lo;
     }
     const double t = 0.5 * (lo + hi);
-    if (lane == 0) {
-        // Inverse iteration: one factorisation of T - shift I, four solves.
+    if (tid == 0) {
+        // Inverse iteration from a shift within a few ulps of theta: one
+        // factorisation of T - shift I, two solves.
         const double tiny = eps * fmax(tnorm, 2.2250738585072014e-308);
         const double shift = t + 4.0 * eps * fmax(tnorm, fabs(t));
         tridiag_factor(d, e, m, shift, tiny, work);
         for (int64_t i = 0; i < m; ++i) u[i] = 1.0;
-        for (int it = 0; it < 4; ++it) {
+        for (int iter = 0; iter < 2; ++iter) {
             tridiag_apply(m, work, u);
             double s = 0.0;
             for (int64_t i = 0; i < m; ++i) s += u[i] * u[i];
