@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "convert.h"
 #include "tridiag.cuh"
 
 
@@ -37,7 +38,6 @@ namespace {
 using namespace psdgb;
 
 constexpr int LZ_CLASSES = 4;     // Lanczos CTA sizes 512, 256, 128, 64 threads
-constexpr int kLzThreads[LZ_CLASSES] = {512, 256, 128, 64};
 
 // Lanczos CTA size class of a block of size n: the smallest CTA of at least
 // n threads, between 64 and 512.
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
 // written as FP32 rows (a32, n x ld4) — one CTA per block, 32x32 transposes.
 __global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const double* __restrict__ x,
                                     float* a32) {
-    __shared__ double sm[32][33];
+    __shared__ float sm[32][33];
     const LzBlockDesc d = descs[blockIdx.x];
     if (d.n == 0) return;
     const int n = d.n, ld4 = d.ld4;
@@ -326,15 +326,16 @@ __global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const
         __syncthreads();
         for (int ty = ty0; ty < 32; ty += 8) {
             const int r = rbase + tx, c = cbase + ty;
-            sm[ty][tx] = (r < n && c < n) ? X[r + static_cast<int64_t>(c) * n] : 0.0;
+            // Narrowed on the integer ALUs (convert.h): FP64 issues slowly here.
+            sm[ty][tx] = (r < n && c < n) ? d2f_rn(X[r + static_cast<int64_t>(c) * n]) : 0.0f;
         }
         __syncthreads();
         for (int ty = ty0; ty < 32; ty += 8) {
             const int i = bi * 32 + ty, j = bj * 32 + tx;
             if (i >= n || j >= ld4) continue;
-            double v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
-            if (j >= n) v = 0.0;
-            A[static_cast<int64_t>(i) * ld4 + j] = static_cast<float>(v);
+            float v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
+            if (j >= n) v = 0.0f;
+            A[static_cast<int64_t>(i) * ld4 + j] = v;
         }
     }
 }
@@ -354,10 +355,13 @@ __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlock
                                                                    const double* __restrict__ x, int from_x,
                                                                    SplitMat out, int fmt, int64_t ld) {
     static_assert(COPY_THREADS == 256, "two halves of 128 threads");
-    __shared__ double sm[2][32][33];
+    __shared__ float sm[2][32][33];
     const LzBlockDesc d = lz[blockIdx.x];
     const BlockDesc bd = blocks[blockIdx.x];
-    const double inv = states[blockIdx.x].inv_scale;
+    // The scaling runs in FP32 (as in the single-matrix split) and the FP64
+    // input is narrowed on the integer ALUs (convert.h): FP64 instructions
+    // issue slowly on this GPU.
+    const float inv = d2f_rn(states[blockIdx.x].inv_scale);
     const int n = d.n, np = bd.np;
     const int h = threadIdx.x / 128, ht = threadIdx.x % 128;
     const int tx = ht % 32, ty0 = ht / 32;        // load phase: 32 x 4
@@ -377,7 +381,7 @@ __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlock
             __syncthreads();
             for (int ty = ty0; ty < 32; ty += 4) {
                 const int rr = rbase + tx, c = cbase + ty;
-                sm[h][ty][tx] = (valid && rr < n && c < n) ? X[rr + static_cast<int64_t>(c) * n] : 0.0;
+                sm[h][ty][tx] = (valid && rr < n && c < n) ? d2f_rn(X[rr + static_cast<int64_t>(c) * n]) : 0.0f;
             }
             __syncthreads();
         }
@@ -388,10 +392,10 @@ __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlock
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
                 const int cl = 8 * g + e;
-                double val = 0.0;
+                float val = 0.0f;
                 if (i < n && j0 + e < n)
                     val = (bi < bj) ? sm[h][cl][r] : (bi > bj) ? sm[h][r][cl] : ((r <= cl) ? sm[h][cl][r] : sm[h][r][cl]);
-                v[e] = static_cast<float>(val * inv);
+                v[e] = val * inv;
             }
         } else if (vec_ok && i < n && j0 + 8 <= n) {
             const float* src = A + static_cast<int64_t>(i) * d.ld4 + j0;
@@ -399,12 +403,12 @@ __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlock
             const float4 u1 = *reinterpret_cast<const float4*>(src + 4);
             const float w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = static_cast<float>(static_cast<double>(w[e]) * inv);
+            for (int e = 0; e < 8; ++e) v[e] = w[e] * inv;
         } else {
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-                const double val = (i < n && j0 + e < n) ? A[static_cast<int64_t>(i) * d.ld4 + j0 + e] : 0.0;
-                v[e] = static_cast<float>(val * inv);
+                const float val = (i < n && j0 + e < n) ? A[static_cast<int64_t>(i) * d.ld4 + j0 + e] : 0.0f;
+                v[e] = val * inv;
             }
         }
         split_store8(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j0, v);

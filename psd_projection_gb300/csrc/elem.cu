@@ -5,6 +5,7 @@
 // src/utils.cu:34-60,106-131, src/composite_FP32.cu:44,184): the FP64 input is
 // read once to build the FP32 copy the Lanczos bound streams, and once more to
 // write the scaled, split filter operand.  All are HBM-bound.
+#include "convert.h"
 #include "internal.h"
 
 namespace psdgb {
@@ -21,12 +22,23 @@ constexpr int TR = 8;   // rows per thread pass
 // coalesced, and writes the row-major output tiles (lo, hi) and (hi, lo)
 // through a shared-memory transpose (only (lo, lo) on the diagonal).  Each
 // upper element is read once: 4 n^2 bytes of FP64 input per matrix.
+//
+// Values are narrowed to FP32 as they are loaded (FP64 inputs on the integer
+// ALUs, convert.h) and scaled in FP32: FP64 instructions issue slowly on this
+// GPU and per-element FP64 work made these kernels FP64-bound.  With scale 1
+// the stored value is exactly the FP32 rounding of the input.
+template <class T>
+__device__ __forceinline__ float narrow(T v) { return static_cast<float>(v); }
+template <>
+__device__ __forceinline__ float narrow<double>(double v) { return d2f_rn(v); }
+
 template <class T, class Store>
 __global__ void __launch_bounds__(TS * TR) sym_upper_tiles(const T* __restrict__ x, int64_t n, int64_t rows_out,
-                                                           int64_t cols_out, double scale, const double* scale_dev,
+                                                           int64_t cols_out, double scale64, const double* scale_dev,
                                                            Store st) {
-    __shared__ double sm[TS][TS + 1];
-    if (scale_dev != nullptr) scale *= *scale_dev;
+    __shared__ float sm[TS][TS + 1];
+    const float scale = d2f_rn(scale_dev != nullptr ? scale64 * *scale_dev : scale64);
+    const bool unscaled = scale == 1.0f;
     // Pair t in row-major order over the tiles (hi, lo), lo <= hi.
     const int64_t t = blockIdx.x;
     // FP32 square root for the estimate (FP64 issues slowly on this GPU); the
@@ -39,21 +51,21 @@ __global__ void __launch_bounds__(TS * TR) sym_upper_tiles(const T* __restrict__
     const int64_t rbase = lo * TS, cbase = hi * TS;
     for (int ty = ty0; ty < TS; ty += TR) {
         const int64_t r = rbase + tx, c = cbase + ty;
-        sm[ty][tx] = (r < n && c < n) ? static_cast<double>(x[r + c * n]) : 0.0;  // X(rbase+tx, cbase+ty)
+        sm[ty][tx] = (r < n && c < n) ? narrow<T>(x[r + c * n]) : 0.0f;  // X(rbase+tx, cbase+ty)
     }
     __syncthreads();
     for (int ty = ty0; ty < TS; ty += TR) {
         {   // tile (lo, hi): X(i, j) with i = rbase + ty <= j = cbase + tx (or the diagonal block)
             const int64_t i = rbase + ty, j = cbase + tx;
-            double v = (lo < hi || ty <= tx) ? sm[tx][ty] : sm[ty][tx];
-            if (i >= n || j >= n) v = 0.0;
-            if (i < rows_out && j < cols_out) st(i, j, v * scale);
+            float v = (lo < hi || ty <= tx) ? sm[tx][ty] : sm[ty][tx];
+            if (i >= n || j >= n) v = 0.0f;
+            if (i < rows_out && j < cols_out) st(i, j, unscaled ? v : v * scale);
         }
         if (lo < hi) {  // tile (hi, lo): X(i, j) = X(j, i), i = cbase + ty, j = rbase + tx
             const int64_t i = cbase + ty, j = rbase + tx;
-            double v = sm[ty][tx];
-            if (i >= n || j >= n) v = 0.0;
-            if (i < rows_out && j < cols_out) st(i, j, v * scale);
+            float v = sm[ty][tx];
+            if (i >= n || j >= n) v = 0.0f;
+            if (i < rows_out && j < cols_out) st(i, j, unscaled ? v : v * scale);
         }
     }
 }
@@ -68,15 +80,15 @@ inline unsigned pair_blocks(int64_t rows_out, int64_t cols_out) {
 struct StoreF32 {
     float* a;
     int64_t ld;
-    __device__ void operator()(int64_t i, int64_t j, double v) const { a[i * ld + j] = static_cast<float>(v); }
+    __device__ void operator()(int64_t i, int64_t j, float v) const { a[i * ld + j] = v; }
 };
 
 struct StoreSplit {
     SplitMat m;
     int fmt;
     int64_t np;
-    __device__ void operator()(int64_t i, int64_t j, double v) const {
-        split_store(m, fmt, static_cast<size_t>(i * np + j), static_cast<float>(v));
+    __device__ void operator()(int64_t i, int64_t j, float v) const {
+        split_store(m, fmt, static_cast<size_t>(i * np + j), v);
     }
 };
 
