@@ -133,6 +133,9 @@ struct EpiParams {
     int dual;           // mainloop: accumulate P*Q^T + Q*P^T (K doubled), the symmetric part of the product
     float acc_scale;    // the accumulator is multiplied by this first (0.5 for a dual product)
     int ld;             // row stride of the split-matrix layout (elements); np for a single matrix
+    int skip_pad;       // EPI_STORE / EPI_STEP: leave 32 x 32 runs wholly outside the block's n x n
+                        // alone (their operand values are zero and stay zero: only set where the
+                        // padding of every split matrix is zero, as in the batch layout)
 };
 
 // A group of independent blocks sharing one strided operand layout: block b

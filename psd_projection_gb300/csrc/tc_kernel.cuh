@@ -263,6 +263,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
         }
         return;
     }
+    if (ep.skip_pad && (p0 >= ti.blk.n || q0 >= ti.blk.n)) return;  // padding run (warp-uniform)
     const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
