@@ -107,7 +107,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         bool stop = false;
         for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_half = ti.blk.np / BK;
+            const int kb_half = tile_kblocks(ep, ti);
             const int kb_total = kb_half * dual_mult;
             const int row_p = static_cast<int>(ti.blk.row_base + ti.bi * BM);
             const int row_q = static_cast<int>(ti.blk.row_base + ti.bj * BN);
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         bool stop = false;
         for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_total = (ti.blk.np / BK) * dual_mult;
+            const int kb_total = tile_kblocks(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
             if (!mbar_wait_bounded(&acc_empty[buf], use_ph ^ 1u)) {
@@ -193,7 +193,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         int it = 0;
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_total = (ti.blk.np / BK) * dual_mult;
+            const int kb_total = tile_kblocks(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
             if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {

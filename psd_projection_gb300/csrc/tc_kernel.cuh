@@ -119,6 +119,16 @@ __device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiPara
     return ti;
 }
 
+// K blocks of one half of a tile's K loop: np / BK, or, where the operands'
+// padding is zero (ep.skip_pad), only the blocks that reach into the block's
+// n columns (the rest multiply zeros).  Producer, MMA issuer and epilogue
+// all use this count.
+__device__ __forceinline__ int tile_kblocks(const EpiParams& ep, const TileInfo& ti) {
+    if (!ep.skip_pad) return ti.blk.np / BK;
+    const int kb = (ti.blk.n + BK - 1) / BK;
+    return kb < 1 ? 1 : kb;
+}
+
 __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag, int code) {
     *abort_flag = 1;
     atomicCAS(err, 0, code);
