@@ -95,7 +95,11 @@ int psdgb_filter_coefficients(int schedule, float* out, int cap);
  * ws == NULL, or ws_bytes below this size, gets the library's own cached
  * workspace (allocated on first use, grown on demand and kept until
  * psdgb_release_workspace or process exit).  The Lanczos state (a few
- * n-vectors and the n x max_iter basis) always comes from a cached buffer. */
+ * n-vectors and the n x max_iter basis) always comes from a cached buffer.
+ * A caller workspace (and a caller Lanczos state) must be 16-byte aligned
+ * (cudaMalloc gives 256): the kernels read it through TMA tensor maps and
+ * 16-byte vectors; an unaligned one is refused with
+ * PSDGB_ERR_INVALID_ARGUMENT before any work is enqueued. */
 size_t psdgb_composite_workspace_size(int64_t n, int precision);
 psdgb_status psdgb_release_workspace(void);
 
@@ -129,7 +133,9 @@ psdgb_status psdgb_composite_auto_scale(int precision, int schedule, double* d_m
                                         void* d_ws, size_t ws_bytes, void* stream,
                                         double* up_out);
 
-/* Bytes of the Lanczos state (a few n-vectors and the n x max_iter basis). */
+/* Bytes of the Lanczos state (a few n-vectors, the n x max_iter basis, the
+ * tridiagonal solver's scratch and, for the triangle-tile matvec, the FP64
+ * partial sums: n^2 / 16 bytes). */
 size_t psdgb_lanczos_state_size(int64_t n, int64_t max_iter);
 
 /* psdgb_composite_auto_scale without any host synchronisation: the Lanczos
