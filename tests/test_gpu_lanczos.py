@@ -148,3 +148,35 @@ def test_triangle_matvec_large(psd, matvec_mode):
     assert out[1]["lo"] == pytest.approx(out[0]["lo"], rel=1e-6)
     assert out[1]["up"] == pytest.approx(out[0]["up"], rel=1e-4)
     assert out[1]["lo"] <= out[1]["up"]
+
+
+@pytest.mark.parametrize("kind", ["gaussian", "clustered_top", "rank_two"])
+@pytest.mark.parametrize("n", [300, 2100])
+def test_tridiagonal_top_eigenvalue(psd, kind, n):
+    """theta (the largest eigenvalue of the Lanczos tridiagonal, found by the
+    four-warp Sturm multisection) against LAPACK on the same tridiagonal built
+    from the returned alpha / beta: agreement to 32 ulps of ||T|| (both
+    carry rounding errors of a few ulps of ||T||), also
+    when the top of the spectrum is clustered (a near-double eigenvalue of
+    A^T A) or when the recurrence stops early."""
+    rng = np.random.default_rng(n + len(kind))
+    if kind == "gaussian":
+        a = gaussian_sym(n, seed=n + 3)
+    elif kind == "clustered_top":
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        lam = rng.uniform(-1.0, 1.0, n)
+        lam[:3] = [2.0, -2.0 + 1e-9, 2.0 - 1e-9]
+        a = (q * lam) @ q.T
+        a = 0.5 * (a + a.T)
+    else:
+        u, v = rng.standard_normal(n), rng.standard_normal(n)
+        a = np.outer(u, u) - 0.5 * np.outer(v, v)
+    got = psd.lanczos_details(to_dev(a), 20, 1e-10)
+    m = got["nb_iter"]
+    assert m >= 1
+    al = np.array(got["alpha"][:m])
+    be = np.array(got["beta"][:m])
+    t = np.diag(al) + np.diag(be[: m - 1], 1) + np.diag(be[: m - 1], -1)
+    want = np.linalg.eigvalsh(t)[-1]
+    tnorm = np.abs(t).sum(axis=1).max()
+    assert abs(got["theta"] - want) <= 32 * np.finfo(float).eps * tnorm
