@@ -337,10 +337,12 @@ psdgb_status psdgb_composite_auto_scale_deflate_two_ends(int precision, int sche
 
 /* A sequence of `count` n x n host matrices (h_in[i] -> h_out[i]; a buffer
  * may appear more than once and h_out[i] may equal h_in[i], but h_out[i] must
- * not be h_in[i + 1], which is read while matrix i is projected) with one
- * method, pipelined: the host-to-device copy of matrix i + 1 and the
- * device-to-host copy of matrix i - 1 run on their own streams while matrix i
- * is projected on `stream`, through two device staging matrices.  Copies
+ * not be h_in[i + 1] or h_in[i + 2], which may be read while matrix i is
+ * projected or copied back) with one method, pipelined: the host-to-device
+ * copies of the next matrices and the device-to-host copy of matrix i - 1 run
+ * on their own streams while matrix i is projected on `stream`, through three
+ * device staging matrices (an upload waits only for the download three steps
+ * earlier).  Copies
  * overlap only for page-locked host buffers (cudaHostAlloc / cudaHostRegister).
  * Returns after the last result is in host memory.  The EVD methods run the
  * matrices one after the other.  No counterpart in the reference, whose

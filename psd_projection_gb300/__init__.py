@@ -240,7 +240,8 @@ def project_host_many(method: str, inputs, outputs, stream=None):
     """Project a sequence of (n, n) float64 host matrices (numpy arrays or
     pinned CPU tensors, column-major) with one method: inputs[i] -> outputs[i],
     the copies of neighbouring matrices overlapping each projection
-    (psdgb_project_host_many).  outputs[i] must not be inputs[i + 1]."""
+    (psdgb_project_host_many).  outputs[i] must not be inputs[i + 1] or
+    inputs[i + 2] (refused with PsdgbError)."""
     import numpy as np
 
     torch = _torch()

@@ -337,8 +337,9 @@ psdgb_status psdgb_release_workspace(void) {
         DeviceState* ds = kv.second;
         if (ds->ws) cudaFree(ds->ws);
         if (ds->lz) cudaFree(ds->lz);
-        ds->ws = ds->lz = nullptr;
-        ds->ws_bytes = ds->lz_bytes = 0;
+        if (ds->stage2) cudaFree(ds->stage2);
+        ds->ws = ds->lz = ds->stage2 = nullptr;
+        ds->ws_bytes = ds->lz_bytes = ds->stage2_bytes = 0;
     }
     return PSDGB_OK;
 }
@@ -596,6 +597,14 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
     if (!h_in || !h_out) { set_error("null host buffer list"); return PSDGB_ERR_INVALID_ARGUMENT; }
     for (int64_t i = 0; i < count; ++i)
         if (!h_in[i] || !h_out[i]) { set_error("null host buffer"); return PSDGB_ERR_INVALID_ARGUMENT; }
+    // The uploads of the next two matrices may run while result i is copied
+    // back, so a result may not land in either of their inputs.
+    for (int64_t i = 0; i < count; ++i)
+        for (int64_t j = i + 1; j <= i + 2 && j < count; ++j)
+            if (static_cast<const void*>(h_out[i]) == static_cast<const void*>(h_in[j])) {
+                set_error("psdgb_project_host_many: h_out[i] must not be h_in[i + 1] or h_in[i + 2]");
+                return PSDGB_ERR_INVALID_ARGUMENT;
+            }
     if (eig64 >= 0) {
         for (int64_t i = 0; i < count; ++i) PSDGB_TRY(psdgb_project_host(method, h_in[i], h_out[i], n, nullptr, stream));
         return PSDGB_OK;
@@ -607,7 +616,7 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
     if (!ds->copy_in) {
         PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&ds->copy_in, cudaStreamNonBlocking));
         PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&ds->copy_out, cudaStreamNonBlocking));
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < DeviceState::kHostStages; ++b) {
             PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->in_done[b], cudaEventDisableTiming));
             PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->comp_done[b], cudaEventDisableTiming));
             PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&ds->out_done[b], cudaEventDisableTiming));
@@ -615,7 +624,12 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
     }
     const size_t bytes = sizeof(double) * static_cast<size_t>(n) * n;
     const size_t stride = (bytes + 255) / 256 * 256;
-    PSDGB_TRY(ensure_buffer(&ds->stage2, &ds->stage2_bytes, 2 * stride));
+    // Three staging matrices: the upload of step i waits only for the
+    // download of step i - 3, so uploads and downloads (two copy streams)
+    // both overlap the projections even when a host copy takes most of a
+    // projection's time.
+    constexpr int S = DeviceState::kHostStages;
+    PSDGB_TRY(ensure_buffer(&ds->stage2, &ds->stage2_bytes, S * stride));
     void *ws = nullptr, *lz = nullptr;
     PSDGB_TRY(resolve_ws(ds, n, precision, nullptr, 0, &ws));
     PSDGB_TRY(resolve_lz(ds, n, 20, &lz));
@@ -625,9 +639,9 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
     PSDGB_CUDA_TRY(cudaEventRecord(ds->comp_done[0], s));
     PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_in, ds->comp_done[0], 0));
     for (int64_t i = 0; i < count; ++i) {
-        const int b = static_cast<int>(i & 1);
+        const int b = static_cast<int>(i % S);
         double* d = reinterpret_cast<double*>(static_cast<char*>(ds->stage2) + b * stride);
-        if (i >= 2) PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_in, ds->out_done[b], 0));
+        if (i >= S) PSDGB_CUDA_TRY(cudaStreamWaitEvent(ds->copy_in, ds->out_done[b], 0));
         PSDGB_CUDA_TRY(cudaMemcpyAsync(d, h_in[i], bytes, cudaMemcpyHostToDevice, ds->copy_in));
         PSDGB_CUDA_TRY(cudaEventRecord(ds->in_done[b], ds->copy_in));
         PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->in_done[b], 0));
@@ -638,7 +652,7 @@ psdgb_status psdgb_project_host_many(const char* method, const double* const* h_
         PSDGB_CUDA_TRY(cudaMemcpyAsync(h_out[i], d, bytes, cudaMemcpyDeviceToHost, ds->copy_out));
         PSDGB_CUDA_TRY(cudaEventRecord(ds->out_done[b], ds->copy_out));
     }
-    PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->out_done[(count - 1) & 1], 0));
+    PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, ds->out_done[(count - 1) % S], 0));
     return finish(ds, s);
 }
 

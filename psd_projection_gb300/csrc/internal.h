@@ -41,9 +41,10 @@ struct DeviceState {
     int sm_count = 0;
     int cc_major = 0, cc_minor = 0;
     // Host-sequence projections (psdgb_project_host_many): copy streams,
-    // ordering events and two staging matrices, created on first use.
+    // ordering events and kHostStages staging matrices, created on first use.
+    static constexpr int kHostStages = 3;
     cudaStream_t copy_in = nullptr, copy_out = nullptr;
-    cudaEvent_t in_done[2] = {nullptr, nullptr}, comp_done[2] = {nullptr, nullptr}, out_done[2] = {nullptr, nullptr};
+    cudaEvent_t in_done[kHostStages] = {}, comp_done[kHostStages] = {}, out_done[kHostStages] = {};
     void* stage2 = nullptr;
     size_t stage2_bytes = 0;
 };

@@ -84,7 +84,7 @@ def test_kernel_launches_are_counted(psd):
 
 def test_project_host_many_matches_one_call_per_matrix():
     """The pipelined host sequence (copies of neighbouring matrices
-    overlapping each projection, two staging buffers) returns, for every
+    overlapping each projection, three staging buffers) returns, for every
     matrix, exactly what one synchronous call returns: the same device path
     runs on the same input.  Buffers rotate (a buffer reused three steps
     later) and one result overwrites its own input."""
@@ -122,3 +122,7 @@ def test_project_host_many_validates():
         psd.project_host_many("composite_FP32", [a], [])
     with pytest.raises(psd.PsdgbError, match="Unknown method"):
         psd.project_host_many("nope", [a], [np.zeros((4, 4))])
+    # A result may not land in the input of either of the next two matrices.
+    bufs = [np.eye(4) for _ in range(3)]
+    with pytest.raises(psd.PsdgbError, match="must not be"):
+        psd.project_host_many("composite_FP32", bufs, [bufs[2], np.zeros((4, 4)), np.zeros((4, 4))])
