@@ -55,6 +55,28 @@ def test_batch_matches_one_call_per_block():
             assert rp.rel_frobenius(y, proj) <= 1e-4, n
 
 
+def test_batch_large_blocks():
+    """Blocks above 512 (up to the 4096 limit) run their Lanczos bound in the
+    512-thread class with more than 48 KB of shared memory, next to tiny
+    ones; each block matches one call per block."""
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    sizes = [700, 20, 1030, 3]
+    mats = _blocks(sizes, seed=4)
+    d = pack(mats)
+    with BatchPlan(sizes) as plan:
+        plan.project(d)
+        import torch
+
+        torch.cuda.synchronize()
+    got = unpack(d, sizes)
+    for n, x, y in zip(sizes, mats, got):
+        t = to_dev(x)
+        psd.composite_FP32_auto_scale(t)
+        assert rp.rel_frobenius(y, from_dev(t)) <= 1e-5, n
+
+
 def test_batch_graph_replay_and_autotune():
     import torch
 

@@ -180,3 +180,23 @@ def test_tridiagonal_top_eigenvalue(psd, kind, n):
     want = np.linalg.eigvalsh(t)[-1]
     tnorm = np.abs(t).sum(axis=1).max()
     assert abs(got["theta"] - want) <= 32 * np.finfo(float).eps * tnorm
+
+
+def test_long_recurrence_tridiagonal_in_global_scratch(psd):
+    """max_iter = 800: the tridiagonal solver's staged T and LU no longer fit
+    its shared-memory allotment and live in the Lanczos state instead; theta
+    still matches LAPACK on the returned coefficients and the bound brackets
+    the two-norm."""
+    n = 1000
+    a = gaussian_sym(n, seed=17)
+    got = psd.lanczos_details(to_dev(a), 800, 1e-10)
+    m = got["nb_iter"]
+    assert m > 760
+    al = np.array(got["alpha"][:m])
+    be = np.array(got["beta"][:m])
+    t = np.diag(al) + np.diag(be[: m - 1], 1) + np.diag(be[: m - 1], -1)
+    want = np.linalg.eigvalsh(t)[-1]
+    tnorm = np.abs(t).sum(axis=1).max()
+    assert abs(got["theta"] - want) <= 64 * np.finfo(float).eps * tnorm
+    sigma = np.linalg.norm(a, 2)
+    assert got["lo"] <= sigma * (1 + 1e-5) and got["up"] >= sigma * (1 - 1e-6)
