@@ -77,16 +77,23 @@ def parse_args():
 # ---------------------------------------------------------------------------
 
 def dist_setup():
+    """Rank and world size from the torchrun environment; one process per GPU
+    over NCCL (gloo on a host without GPUs, where only the plumbing runs)."""
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
+    cuda = torch.cuda.is_available()
+    if cuda:
+        torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
 
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        if cuda:
+            dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        else:
+            dist.init_process_group("gloo")
     return rank, world
 
 
@@ -98,14 +105,22 @@ def barrier(world):
 
 
 def max_over_ranks(x: float, world: int) -> float:
+    """The largest x over the ranks (every rank gets it)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ms_max: float, world: int) -> float:
+    """Units of all ranks per second over the slowest rank's time: each of the
+    `world` replicas processed `units_per_rank` units in at most ms_max ms."""
+    return world * units_per_rank / (ms_max / 1e3)
 
 
 # ---------------------------------------------------------------------------
@@ -629,7 +644,7 @@ def run_ours(args, rank, world):
     err = psd.rel_frobenius(inputs[W + K - 1], P) if P is not None else None
     clocks = clk.summary()
 
-    value = world * K / (ms_total / 1e3)
+    value = whole_job_rate(K, ms_total, world)
     steps_filter = 7 if sched == psd.SCHEDULE_FP16 else 10
     tc = {
         "dense_equiv_tflops": value / world * dense_equiv_flops(n, steps_filter) / 1e12,
