@@ -16,10 +16,13 @@ Arms:
                      `e2e` runs psdgb_project_host_many("composite_FP32") on pinned
                      host buffers with both copies inside the timed region.
   --impl reference   the reference's CPU path named by the goal: FP64 LAPACK
-                     dsyevd EVD projection (eig_FP64_psd's math) on all host
-                     cores, on a bounded n = 4096 sample scaled by n^3; plus
-                     a replay of the reference's own cuBLAS call sequence for
-                     composite_FP32_auto_scale (plain FP32 Sgemm) on the GPU.
+                     dsyevd EVD projection (eig_FP64_psd's math) of the full
+                     n = 8192 matrix on all host cores, one per step; plus the
+                     reference's three GPU methods (composite_FP32 on FP32
+                     Sgemm, composite_FP16 on FP16 GemmEx, composite_FP32_emulated
+                     on cuBLAS's BF16x9 emulation, each auto-scaled) replayed
+                     call for call on cuBLAS / cuSOLVER, with the reference's
+                     per-call allocation and with caller workspaces.
 
 Multi-GPU: a single projection does not shard, so N GPUs run N independent
 replicas (one process per GPU under torchrun) and `value` is N x steps over
@@ -58,7 +61,6 @@ def parse_args():
     ap.add_argument("--precision", default="fp16x3")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-side-by-side", action="store_true")
-    ap.add_argument("--cpu-sample-n", type=int, default=4096)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving session")
     ap.add_argument("--no-batch", action="store_true", help="skip the block-diagonal batch session")
     ap.add_argument("--only-batch", action="store_true", help="run only the block-diagonal batch session")
@@ -575,21 +577,33 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
 # CPU baseline: FP64 LAPACK dsyevd projection (eig_FP64_psd's math)
 # ---------------------------------------------------------------------------
 
-def cpu_evd_projection_rate(X, n_full: int, n_sample: int, repeats: int = 1):
-    import numpy as np
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), for the baseline records."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        fields = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+        name = fields.get("Model name", "").strip()
+        vendor = fields.get("Vendor ID", "").strip()
+        return " ".join(x for x in (vendor, name) if x) or "unknown"
+    except (OSError, subprocess.SubprocessError, ValueError):
+        return "unknown"
 
+
+def cpu_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_evd_projection_time(xs) -> float:
+    """Seconds for one FP64 LAPACK dsyevd projection V max(L, 0) V^T of the
+    full host matrix xs (scipy eigh 'evd', all host cores)."""
     from oracle import reference_port as rp
 
-    xs = X[:n_sample, :n_sample].cpu().numpy()
-    xs = 0.5 * (xs + xs.T)
-    times = []
-    for _ in range(repeats):
-        t0 = time.perf_counter()
-        rp.eig_psd(xs)
-        times.append(time.perf_counter() - t0)
-    t = min(times)
-    scale = (n_full / n_sample) ** 3
-    return 1.0 / (t * scale), t, scale
+    t0 = time.perf_counter()
+    rp.eig_psd(xs)
+    return time.perf_counter() - t0
 
 
 # ---------------------------------------------------------------------------
@@ -777,11 +791,12 @@ def run_ours(args, rank, world):
             "sessions": sessions}
 
     if world == 1 and not args.no_cpu_baseline:
-        rate, t, scale = cpu_evd_projection_rate(X, n, args.cpu_sample_n)
-        out["cpu_baseline"] = {"value": rate, "unit": "proj/s", "cores": os.cpu_count(), "kind": "port",
-                               "sample": f"FP64 LAPACK dsyevd projection V max(L,0) V^T (scipy eigh 'evd') of "
-                                         f"the leading {args.cpu_sample_n}^2 block, {t:.2f} s, scaled by "
-                                         f"(n/{args.cpu_sample_n})^3 = {scale:g}"}
+        xs = X.cpu().numpy()
+        t = cpu_evd_projection_time(xs)
+        out["cpu_baseline"] = {"value": 1.0 / t, "unit": "proj/s", "cores": cpu_cores(), "cpu": cpu_model(),
+                               "kind": "port",
+                               "sample": f"one FP64 LAPACK dsyevd projection V max(L,0) V^T (scipy eigh 'evd') of "
+                                         f"the full {n}x{n} matrix, {t:.2f} s"}
     return out
 
 
@@ -792,52 +807,71 @@ def run_reference(args, rank, world):
         return None
     n, K, W = args.n, args.steps, args.warmup
     X, P, _ = make_workload(n, seed=0)
-    # CPU path: FP64 dsyevd projection on all host cores, bounded sample, scaled by n^3.
+    xs = X.cpu().numpy()
+    # CPU path: one full FP64 dsyevd projection per step, on all host cores.
     for _ in range(W):
-        cpu_evd_projection_rate(X, n, args.cpu_sample_n)
+        cpu_evd_projection_time(xs)
     t0 = time.perf_counter()
-    rates = []
-    for _ in range(K):
-        r, _, scale = cpu_evd_projection_rate(X, n, args.cpu_sample_n)
-        rates.append(r)
+    times = [cpu_evd_projection_time(xs) for _ in range(K)]
     wall = time.perf_counter() - t0
-    value = statistics.median(rates)
+    value = K / wall
     out = {
         "metric": METRIC, "value": value, "unit": "proj/s", "n_gpus": 1, "steps": K, "warmup": W,
-        "ms_per_step": 1e3 / value, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": 1e3 * wall / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (same workload as the default arm)", "impl": "reference",
         "config": {"workload": f"single dense projection n={n} (lambda uniform in [-1,1])", "n": n},
-        "cpu_baseline": {"value": value, "unit": "proj/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"FP64 LAPACK dsyevd projection of the leading {args.cpu_sample_n}^2 block per "
-                                   f"step, scaled by (n/{args.cpu_sample_n})^3 = {scale:g}; {K} steps in "
-                                   f"{wall:.1f} s"},
+        "cpu_baseline": {"value": value, "unit": "proj/s", "cores": cpu_cores(), "cpu": cpu_model(), "kind": "port",
+                         "sample": f"one FP64 LAPACK dsyevd projection V max(L,0) V^T (scipy eigh 'evd') of the "
+                                   f"full {n}x{n} matrix per step; {K} steps in {wall:.1f} s (min "
+                                   f"{min(times):.2f} s, max {max(times):.2f} s)"},
         "e2e": {"value": value, "unit": "proj/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    # The reference's own GPU method (plain FP32 composite), replayed on cuBLAS.
-    try:
-        from oracle import gpu_replay
-
-        torch.backends.cuda.matmul.allow_tf32 = False
-        t = X.clone()
-        gpu_replay.composite_fp32_auto_scale_(t)
-        torch.cuda.synchronize()
-        reps = 2
-        ts = [X.clone() for _ in range(reps)]
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for t in ts:
-            gpu_replay.composite_fp32_auto_scale_(t)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / reps
-        err = float(torch.linalg.matrix_norm(ts[-1] - P) / torch.linalg.matrix_norm(P))
-        out["gpu_fp32_composite_replay"] = {
-            "proj_s": 1e3 / ms, "ms": ms, "rel_frobenius_err": err,
-            "what": "composite_FP32_auto_scale call sequence (cuBLAS FP32 Sgemm, TF32 off; FP64 Dgemv Lanczos) "
-                    "replayed through torch on the GPU"}
-    except Exception as exc:  # noqa: BLE001 - report, do not fail the CPU arm
-        out["gpu_fp32_composite_replay"] = {"unavailable": repr(exc)[:200]}
+    if not args.no_side_by_side:
+        out["gpu_methods"] = reference_gpu_methods(X, P)
     return out
+
+
+def reference_gpu_methods(X, P, reps: int = 2) -> dict:
+    """The reference's three auto-scaled GPU methods replayed on cuBLAS /
+    cuSOLVER (oracle/ref_replay.cu) on the same matrix: proj/s as shipped
+    (cudaMalloc / cudaFree inside every call) and with caller workspaces, and
+    the relative Frobenius error against the exact projection."""
+    import torch
+
+    from oracle import gpu_replay
+
+    res = {}
+    for method in ("composite_FP32", "composite_FP16", "composite_FP32_emulated"):
+        try:
+            row = {}
+            ws = gpu_replay.Workspaces(method, X.shape[0])
+            for mode, w in (("per_call_alloc", None), ("caller_workspace", ws)):
+                t = X.clone()
+                gpu_replay.auto_scale(method, t, w)  # warm (handles, kernels, allocator)
+                ts = [X.clone() for _ in range(reps)]
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                for t in ts:
+                    gpu_replay.auto_scale(method, t, w)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                err = float(torch.linalg.matrix_norm(ts[-1] - P) / torch.linalg.matrix_norm(P))
+                row[mode] = {"proj_s": 1e3 / ms, "ms": ms, "rel_frobenius_err": err}
+                del ts
+            del ws
+            row["what"] = {"composite_FP32": "cublasSgemm chain (FP32, default math mode)",
+                           "composite_FP16": "cublasGemmEx FP16 x FP16 -> FP32, CUBLAS_COMPUTE_32F_FAST_16F",
+                           "composite_FP32_emulated": "cublasGemmEx FP32, CUBLAS_COMPUTE_32F_EMULATED_16BFX9"}[method]
+            res[method + "_auto_scale"] = row
+        except Exception as exc:  # noqa: BLE001 - report, do not fail the CPU arm
+            res[method + "_auto_scale"] = {"unavailable": repr(exc)[:300]}
+        torch.cuda.empty_cache()
+    res["how"] = ("oracle/ref_replay.cu: the reference's cuBLAS / cuSOLVER call sequence (Lanczos with host reads "
+                  "of every Ddot / Dnrm2, the GEMM chain, Sgeam symmetrisation, blocking conversions) on the "
+                  "legacy default stream; CUDA events around `reps` calls after one warm call")
+    return res
 
 
 def main():

@@ -110,17 +110,21 @@ psdgb_status psdgb_release_workspace(void);
 psdgb_status psdgb_composite(int precision, int schedule, double* d_mat, int64_t n,
                              void* d_ws, size_t ws_bytes, void* stream);
 
-/* psdgb_composite for callers that cannot allocate device memory (a solver
- * that reserves the GPU's memory up front, a real-time loop that may not wait
- * on or fail in the allocator, code running under stream capture): the
- * operand scratch is a file-scope device array the library reserves at load
- * time, so this call allocates nothing.  No counterpart in the reference.
+/* psdgb_composite for callers that cannot allocate device memory: a solver
+ * that reserves the GPU's memory up front and hands out only its own buffers,
+ * or a real-time loop that may not wait on, or fail in, the allocator.  The
+ * operand scratch is a file-scope device array inside this library's CUDA
+ * module, so the call allocates nothing.  No counterpart in the reference.
  * Limits: precision PSDGB_PREC_FP16 or PSDGB_PREC_FP16X3 and n <= 512 (the
  * array is 3 MiB, held on every GPU that loads the library until exit);
  * larger n returns PSDGB_ERR_INVALID_ARGUMENT.  The first call on a device
- * looks up the array's address; make it before any stream capture.  All calls
- * share the array: overlapping calls on the GPU would race (this library
- * serialises its own calls, each returning after its stream finishes). */
+ * does the set-up: it looks up the array's device address, and (CUDA loads
+ * modules lazily) that lookup loads the module that holds the array, which
+ * takes device memory once.  Make that first call before any stream capture
+ * and before reserving the GPU's memory.  All calls share the array, which
+ * keeps the last call's contents: calls that overlap on the GPU race on it
+ * (this library serialises its own calls; each waits for its stream before
+ * returning, on the error path too). */
 psdgb_status psdgb_composite_static(int precision, int schedule, double* d_mat, int64_t n, void* stream);
 
 /* Lanczos bound, scale by 1/up, filter, and rescale by up
@@ -162,9 +166,10 @@ psdgb_status psdgb_composite_auto_scale_async(int precision, int schedule, doubl
  * tensor-core precision), and the final reconstruction computes in FP64 and
  * writes FP32: the FP64 path's result rounded to FP32, with half its HBM and
  * host-copy traffic.  Warm start / Ritz output as in
- * psdgb_composite_auto_scale_async.  Asynchronous: no host synchronisation;
- * d_ws / d_lanczos may be null (the library's cached buffers are used, so the
- * call must not race another call that uses them). */
+ * psdgb_composite_auto_scale_async.  Asynchronous (no host synchronisation)
+ * when the caller passes both workspaces; d_ws / d_lanczos may be null or too
+ * small, and the library's cached buffers are then used and the call waits
+ * for its stream before returning, so later calls can reuse those buffers. */
 psdgb_status psdgb_composite_auto_scale_f32(int precision, int schedule, float* d_mat, int64_t n, int64_t max_iter,
                                             double tol, uint64_t seed, int residual_mode, const double* d_warm_start,
                                             double* d_ritz_out, void* d_ws, size_t ws_bytes, void* d_lanczos,

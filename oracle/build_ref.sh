@@ -2,11 +2,13 @@
 # Build the reference library (ComputationalRobotics/psd_projection) from its
 # own sources with nvcc, without its CMake (whose unconditional googletest
 # FetchContent cannot run offline).  Output only into oracle/_ref/.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# REFERENCE_ROOT: the argument, else $PSDGB_REFERENCE_ROOT, else the
+# read-only checkout this recipe was written for.
 # The result is used by the tests to compare exported C++ symbols; it is a
 # CUDA library and is never part of the product path.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${PSDGB_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF" >&2; exit 2; }

@@ -282,6 +282,10 @@ PRECISION_MODEL = {
 }
 
 
+# Factor of the FP16 operand terms (psd_projection_gb300/csrc/common.cuh, kF16Scale).
+F16_SCALE = np.float32(4096.0)
+
+
 def _to_bf16(x: np.ndarray) -> np.ndarray:
     """Round FP32 to BF16 (round to nearest even), returned as FP32."""
     u = np.asarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
@@ -295,9 +299,13 @@ def split_terms(x32: np.ndarray, fmt: str) -> list[np.ndarray]:
     if fmt == "f32":
         return [x32]
     if fmt == "f16":
-        hi = x32.astype(np.float16).astype(np.float32)
-        lo = (x32 - hi).astype(np.float16).astype(np.float32)
-        return [hi, lo]
+        # The kernels split v * 2^12 (F16_SCALE) so that the low term stays a
+        # normal FP16 number, and take the factor out of every product and
+        # load; both scalings are exact, so the terms are returned unscaled.
+        xs = (x32 * F16_SCALE).astype(np.float32)
+        hi = xs.astype(np.float16).astype(np.float32)
+        lo = (xs - hi).astype(np.float16).astype(np.float32)
+        return [(hi / F16_SCALE).astype(np.float32), (lo / F16_SCALE).astype(np.float32)]
     b0 = _to_bf16(x32)
     r1 = (x32 - b0).astype(np.float32)
     b1 = _to_bf16(r1)

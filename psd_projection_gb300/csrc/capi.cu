@@ -221,77 +221,91 @@ psdgb_status do_eig(DeviceState* ds, int fp64, double* d_mat, int64_t n, double*
     }
     const int in = static_cast<int>(n);
     const size_t nn = static_cast<size_t>(n) * n;
-    int* d_info = nullptr;
-    PSDGB_CUDA_TRY(cudaMalloc(&d_info, sizeof(int)));
+    // Every call below is checked; the first failure is kept (st, msg) and
+    // the later steps are skipped, but the buffers are always freed.
     psdgb_status st = PSDGB_OK;
+    std::string msg;
+    auto cuda_ok = [&](cudaError_t e, const char* what) {
+        if (st == PSDGB_OK && e != cudaSuccess) {
+            st = e == cudaErrorMemoryAllocation ? PSDGB_ERR_OUT_OF_MEMORY : PSDGB_ERR_CUDA;
+            msg = std::string("eig: ") + what + ": " + cudaGetErrorString(e);
+        }
+        return st == PSDGB_OK;
+    };
+    auto lib_ok = [&](bool ok, const char* what) {
+        if (st == PSDGB_OK && !ok) {
+            st = PSDGB_ERR_SOLVER;
+            msg = std::string("eig: ") + what + " failed";
+        }
+        return st == PSDGB_OK;
+    };
+    int* d_info = nullptr;
+    cuda_ok(cudaMalloc(&d_info, sizeof(int)), "cudaMalloc(info)");
     if (fp64) {
         // src/eig_FP64_psd.cu:24-85: syevd (upper) -> clip -> V diag(max(w,0)) V^T.
         double *V = nullptr, *W = nullptr, *work = nullptr, *VS = nullptr;
         int lwork = 0;
-        if (cudaMalloc(&V, nn * 8) || cudaMalloc(&VS, nn * 8) || cudaMalloc(&W, n * 8)) {
-            st = PSDGB_ERR_OUT_OF_MEMORY;
-        } else {
-            cudaMemcpyAsync(V, d_mat, nn * 8, cudaMemcpyDeviceToDevice, s);
-            cusolverDnDsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in, W, &lwork);
-            if (cudaMalloc(&work, sizeof(double) * (lwork > 0 ? lwork : 1))) st = PSDGB_ERR_OUT_OF_MEMORY;
-        }
-        if (st == PSDGB_OK &&
-            cusolverDnDsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in, W, work, lwork,
-                             d_info) != CUSOLVER_STATUS_SUCCESS)
-            st = PSDGB_ERR_SOLVER;
-        if (st == PSDGB_OK) {
-            if (d_eigs_out) cudaMemcpyAsync(d_eigs_out, W, n * 8, cudaMemcpyDeviceToDevice, s);
-            cudaMemcpyAsync(VS, V, nn * 8, cudaMemcpyDeviceToDevice, s);
-            if (launch_scale_columns_relu(VS, W, n, s) != cudaSuccess) st = PSDGB_ERR_CUDA;
-            const double one = 1.0, zero = 0.0;
-            if (st == PSDGB_OK && cublasDgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, V, in, &zero,
-                                              d_mat, in) != CUBLAS_STATUS_SUCCESS)
-                st = PSDGB_ERR_SOLVER;
-        }
-        cudaStreamSynchronize(s);
+        cuda_ok(cudaMalloc(&V, nn * 8), "cudaMalloc(V)") && cuda_ok(cudaMalloc(&VS, nn * 8), "cudaMalloc(VS)") &&
+            cuda_ok(cudaMalloc(&W, n * 8), "cudaMalloc(W)") &&
+            cuda_ok(cudaMemcpyAsync(V, d_mat, nn * 8, cudaMemcpyDeviceToDevice, s), "copy of the input") &&
+            lib_ok(cusolverDnDsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in,
+                                               W, &lwork) == CUSOLVER_STATUS_SUCCESS,
+                   "cusolverDnDsyevd_bufferSize") &&
+            cuda_ok(cudaMalloc(&work, sizeof(double) * (lwork > 0 ? lwork : 1)), "cudaMalloc(work)") &&
+            lib_ok(cusolverDnDsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, V, in, W, work,
+                                    lwork, d_info) == CUSOLVER_STATUS_SUCCESS,
+                   "cusolverDnDsyevd") &&
+            (d_eigs_out == nullptr ||
+             cuda_ok(cudaMemcpyAsync(d_eigs_out, W, n * 8, cudaMemcpyDeviceToDevice, s), "copy of the eigenvalues")) &&
+            cuda_ok(cudaMemcpyAsync(VS, V, nn * 8, cudaMemcpyDeviceToDevice, s), "copy of the eigenvectors") &&
+            cuda_ok(launch_scale_columns_relu(VS, W, n, s), "column scaling");
+        const double one = 1.0, zero = 0.0;
+        if (st == PSDGB_OK)
+            lib_ok(cublasDgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, V, in, &zero, d_mat, in) ==
+                       CUBLAS_STATUS_SUCCESS,
+                   "cublasDgemm");
+        cuda_ok(cudaStreamSynchronize(s), "stream synchronisation");
         cudaFree(V); cudaFree(VS); cudaFree(W); cudaFree(work);
     } else {
         // src/eig_FP32_psd.cu:23-96: FP32 copy -> Ssyevd -> clip -> V diag V^T -> FP64.
         float *A = nullptr, *VS = nullptr, *W = nullptr, *work = nullptr, *C = nullptr;
         int lwork = 0;
-        if (cudaMalloc(&A, nn * 4) || cudaMalloc(&VS, nn * 4) || cudaMalloc(&C, nn * 4) || cudaMalloc(&W, n * 4)) {
-            st = PSDGB_ERR_OUT_OF_MEMORY;
-        } else {
-            launch_f64_to_f32(d_mat, A, static_cast<int64_t>(nn), s);
-            cusolverDnSsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in, W, &lwork);
-            if (cudaMalloc(&work, sizeof(float) * (lwork > 0 ? lwork : 1))) st = PSDGB_ERR_OUT_OF_MEMORY;
-        }
-        if (st == PSDGB_OK &&
-            cusolverDnSsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in, W, work, lwork,
-                             d_info) != CUSOLVER_STATUS_SUCCESS)
-            st = PSDGB_ERR_SOLVER;
-        if (st == PSDGB_OK) {
-            if (d_eigs_out) launch_f32_to_f64(W, d_eigs_out, n, s);
-            cudaMemcpyAsync(VS, A, nn * 4, cudaMemcpyDeviceToDevice, s);
-            if (launch_scale_columns_relu_f32(VS, W, n, s) != cudaSuccess) st = PSDGB_ERR_CUDA;
-            const float one = 1.0f, zero = 0.0f;
-            if (st == PSDGB_OK && cublasSgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, A, in, &zero,
-                                              C, in) != CUBLAS_STATUS_SUCCESS)
-                st = PSDGB_ERR_SOLVER;
-            if (st == PSDGB_OK) launch_f32_to_f64(C, d_mat, static_cast<int64_t>(nn), s);
-        }
-        cudaStreamSynchronize(s);
+        cuda_ok(cudaMalloc(&A, nn * 4), "cudaMalloc(A)") && cuda_ok(cudaMalloc(&VS, nn * 4), "cudaMalloc(VS)") &&
+            cuda_ok(cudaMalloc(&C, nn * 4), "cudaMalloc(C)") && cuda_ok(cudaMalloc(&W, n * 4), "cudaMalloc(W)") &&
+            cuda_ok(launch_f64_to_f32(d_mat, A, static_cast<int64_t>(nn), s), "FP32 copy") &&
+            lib_ok(cusolverDnSsyevd_bufferSize(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in,
+                                               W, &lwork) == CUSOLVER_STATUS_SUCCESS,
+                   "cusolverDnSsyevd_bufferSize") &&
+            cuda_ok(cudaMalloc(&work, sizeof(float) * (lwork > 0 ? lwork : 1)), "cudaMalloc(work)") &&
+            lib_ok(cusolverDnSsyevd(h.solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_UPPER, in, A, in, W, work,
+                                    lwork, d_info) == CUSOLVER_STATUS_SUCCESS,
+                   "cusolverDnSsyevd") &&
+            (d_eigs_out == nullptr || cuda_ok(launch_f32_to_f64(W, d_eigs_out, n, s), "eigenvalue conversion")) &&
+            cuda_ok(cudaMemcpyAsync(VS, A, nn * 4, cudaMemcpyDeviceToDevice, s), "copy of the eigenvectors") &&
+            cuda_ok(launch_scale_columns_relu_f32(VS, W, n, s), "column scaling");
+        const float one = 1.0f, zero = 0.0f;
+        if (st == PSDGB_OK)
+            lib_ok(cublasSgemm(h.blas, CUBLAS_OP_N, CUBLAS_OP_T, in, in, in, &one, VS, in, A, in, &zero, C, in) ==
+                       CUBLAS_STATUS_SUCCESS,
+                   "cublasSgemm") &&
+                cuda_ok(launch_f32_to_f64(C, d_mat, static_cast<int64_t>(nn), s), "FP64 conversion");
+        cuda_ok(cudaStreamSynchronize(s), "stream synchronisation");
         cudaFree(A); cudaFree(VS); cudaFree(C); cudaFree(W); cudaFree(work);
     }
     if (st == PSDGB_OK) {
+        // syevd's info: 0 on success, > 0 when the tridiagonal QR did not converge.
         int info = 0;
-        cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost);
-        if (info != 0) {
-            set_error("syevd reported info = " + std::to_string(info));
+        if (cuda_ok(cudaMemcpy(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost), "read of syevd info") &&
+            info != 0) {
             st = PSDGB_ERR_SOLVER;
+            msg = "syevd reported info = " + std::to_string(info) + (info > 0 ? " (no convergence)" : "");
         }
-    } else if (st == PSDGB_ERR_OUT_OF_MEMORY) {
-        set_error("eig: device allocation failed");
-        cudaGetLastError();
-    } else if (st == PSDGB_ERR_SOLVER) {
-        set_error("eig: cuSOLVER/cuBLAS call failed");
     }
     cudaFree(d_info);
+    if (st != PSDGB_OK) {
+        cudaGetLastError();
+        set_error(msg);
+    }
     return st;
 }
 
@@ -422,8 +436,13 @@ psdgb_status psdgb_composite_auto_scale_f32(int precision, int schedule, float* 
     PSDGB_TRY(check_ws_align(d_lanczos, "the Lanczos state"));
     void* lz = d_lanczos;
     if (lz == nullptr || lanczos_bytes < lanczos_state_bytes(n, max_iter)) PSDGB_TRY(resolve_lz(ds, n, max_iter, &lz));
-    return composite_enqueue_f32(ds, precision, schedule, d_mat, n, ws, max_iter, tol, seed, residual_mode, lz,
-                                 static_cast<cudaStream_t>(stream), d_warm_start, d_ritz_out);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    PSDGB_TRY(composite_enqueue_f32(ds, precision, schedule, d_mat, n, ws, max_iter, tol, seed, residual_mode, lz, s,
+                                    d_warm_start, d_ritz_out));
+    // The library's cached buffers are shared with every other call: when this
+    // call took them, it finishes before they can be handed out again.
+    if (ws == ds->ws || lz == ds->lz) return finish(ds, s);
+    return PSDGB_OK;
 }
 
 psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_schedule, int refine_precision,

@@ -28,6 +28,21 @@ struct SplitMat {
     void* term[3];   // device pointers, each Np x Np row-major (ld = Np), zero padded
 };
 
+// FP16 terms hold the value times 2^12.  Unscaled, the low term of an entry
+// below 0.125 in magnitude falls into FP16's subnormal range (below 2^-14),
+// where its absolute spacing 2^-24 caps the hi + lo pair at about 17 bits for
+// the entries of a scaled n = 8192 iterate (about 0.01).  With the factor the
+// low term stays normal for |v| >= 2^-15 and hi + lo carries 22 bits
+// (relative error <= 2^-22) for 3e-5 <= |v| < 16 (65504 / 2^12), which
+// holds the filter operands (their spectral norm, which bounds every entry,
+// is about 1).  The
+// factor is a power of two, so scaling and unscaling are exact: a product of
+// two FP16-format operands accumulates 2^24 times the true value and its
+// epilogue multiplies by 2^-24.
+constexpr float kF16Scale = 4096.0f;
+constexpr float kF16Unscale = 1.0f / 4096.0f;
+constexpr float kF16AccUnscale = 1.0f / 16777216.0f;
+
 __host__ __device__ inline int format_terms(int fmt) { return fmt == FMT_F32 ? 1 : (fmt == FMT_F16 ? 2 : 3); }
 __host__ __device__ inline int format_elem_bytes(int fmt) { return fmt == FMT_F32 ? 4 : 2; }
 
@@ -38,7 +53,7 @@ __device__ __forceinline__ float split_load(const SplitMat& m, int fmt, size_t i
     if (fmt == FMT_F16) {
         const __half* h = static_cast<const __half*>(m.term[0]);
         const __half* l = static_cast<const __half*>(m.term[1]);
-        return __half2float(h[idx]) + __half2float(l[idx]);
+        return (__half2float(h[idx]) + __half2float(l[idx])) * kF16Unscale;
     }
     const __nv_bfloat16* b0 = static_cast<const __nv_bfloat16*>(m.term[0]);
     const __nv_bfloat16* b1 = static_cast<const __nv_bfloat16*>(m.term[1]);
@@ -50,6 +65,7 @@ __device__ __forceinline__ float split_load(const SplitMat& m, int fmt, size_t i
 __device__ __forceinline__ void split_store(const SplitMat& m, int fmt, size_t idx, float v) {
     if (fmt == FMT_F32) { static_cast<float*>(m.term[0])[idx] = v; return; }
     if (fmt == FMT_F16) {
+        v *= kF16Scale;
         __half h = __float2half_rn(v);
         __half l = __float2half_rn(v - __half2float(h));
         static_cast<__half*>(m.term[0])[idx] = h;
@@ -79,8 +95,9 @@ __device__ __forceinline__ void split_store8(const SplitMat& m, int fmt, size_t 
         __align__(16) __half l[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) {
-            h[e] = __float2half_rn(v[e]);
-            l[e] = __float2half_rn(v[e] - __half2float(h[e]));
+            const float x = v[e] * kF16Scale;
+            h[e] = __float2half_rn(x);
+            l[e] = __float2half_rn(x - __half2float(h[e]));
         }
         *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[0]) + idx) = *reinterpret_cast<const uint4*>(h);
         *reinterpret_cast<uint4*>(static_cast<__half*>(m.term[1]) + idx) = *reinterpret_cast<const uint4*>(l);

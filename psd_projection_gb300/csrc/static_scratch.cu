@@ -2,13 +2,11 @@
 // callers that must not allocate device memory.
 //
 // Some callers cannot call cudaMalloc: a solver that reserves the GPU's memory
-// up front and hands out only its own buffers, a real-time loop that may not
-// take the allocator's latency or failure modes, or code that runs the
-// projection while a CUDA stream is being captured into a graph (capture
-// forbids the synchronous allocator).  psdgb_composite needs three operand
-// matrices of scratch and, given no workspace, allocates it.  This entry point
-// instead uses one file-scope device array that the CUDA module reserves
-// when the library is loaded, so a call allocates nothing.
+// up front and hands out only its own buffers, or a real-time loop that may
+// not take the allocator's latency or failure modes.  psdgb_composite needs
+// three operand matrices of scratch and, given no workspace, allocates it.
+// This entry point instead uses one file-scope device array in this file's
+// CUDA module, so a call allocates nothing.
 //
 // Limits and rules:
 //   * n <= kStaticMaxN (512) and the FP16-split precisions only (PSDGB_PREC_FP16,
@@ -16,14 +14,16 @@
 //     (3 MiB) plus an error word.  Every GPU that loads the library holds
 //     this array until the process exits.
 //   * The first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture.
+//     cudaGetSymbolAddress (with that device current).  CUDA loads modules
+//     lazily, so that lookup is also what loads the module holding the array,
+//     which takes device memory once: make the first call before any stream
+//     capture and before the caller reserves the GPU's memory.
 //   * Every call shares the one array, and it keeps the last call's contents.
 //     The operand matrices are fully rewritten by each call (padding included)
 //     and the error word is cleared at the start of each call.  Calls that
 //     overlap on the GPU (another thread, another stream) would race on the
 //     array; calls from this library are serialised by a host lock and each
-//     returns only after its stream has finished.
+//     returns only after its stream has finished, also when it fails.
 #include <mutex>
 #include <string>
 
@@ -105,6 +105,14 @@ extern "C" psdgb_status psdgb_composite_static(int precision, int schedule, doub
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     ds.d_error = reinterpret_cast<int*>(scratch + kStaticOperandBytes);
     PSDGB_CUDA_TRY(cudaMemsetAsync(ds.d_error, 0, sizeof(int), s));
-    PSDGB_TRY(composite_run(&ds, precision, schedule, d_mat, n, scratch, false, 0, 0.0, 0, 0, nullptr, s, nullptr));
+    const psdgb_status st =
+        composite_run(&ds, precision, schedule, d_mat, n, scratch, false, 0, 0.0, 0, 0, nullptr, s, nullptr);
+    if (st != PSDGB_OK) {
+        // Work queued before the failure may still use the array: wait for it
+        // before the lock lets another call in.  The first error is the one reported.
+        cudaStreamSynchronize(s);
+        cudaGetLastError();
+        return st;
+    }
     return finish(&ds, s);
 }

@@ -148,6 +148,10 @@ __device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, c
 #pragma unroll
             for (int j = 0; j < 32; j += 2) {
                 float x0 = v[j], x1 = v[j + 1];
+                if (FMT == FMT_F16) {
+                    x0 *= kF16Scale;
+                    x1 *= kF16Scale;
+                }
                 uint16_t h0 = 0, h1 = 0;
 #pragma unroll
                 for (int u = 0; u <= t; ++u) {
@@ -205,7 +209,8 @@ __device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, in
 }
 
 // Eight consecutive values of a split matrix at element idx (one 16-byte
-// vector per term plane), the terms summed from the smallest to the largest.
+// vector per term plane), the terms summed from the smallest to the largest
+// (FP16 terms: the sum times 2^-12).
 template <int FMT>
 __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (&out)[8]) {
     constexpr int NT = FMT == FMT_F16 ? 2 : 3;
@@ -227,6 +232,10 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
             }
         }
     }
+    if (FMT == FMT_F16) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) out[j] *= kF16Unscale;
+    }
 }
 
 // The epilogue of one 32 x 32 run of accumulator values v (lane = row
@@ -240,6 +249,8 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
     const int64_t rb = ti.blk.row_base;
     const int64_t cb = ti.blk.col_base;
     const int64_t p = p0 + (threadIdx.x & 31);
+    // FP16-format operands carry a factor 2^12 each (kF16Scale).
+    const float acc_scale = FMT == FMT_F16 ? ep.acc_scale * kF16AccUnscale : ep.acc_scale;
     if (ep.kind == EPI_FINAL) {
         const int64_t n = ti.blk.n;
         if (p >= n) return;
@@ -250,7 +261,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
         for (int j = 0; j < 32; ++j) {
             const int64_t q = q0 + j;
             if (q <= p && q < n) {
-                const double o = 0.5 * (x[p * n + q] + up * static_cast<double>(ep.acc_scale * v[j]));
+                const double o = 0.5 * (x[p * n + q] + up * static_cast<double>(acc_scale * v[j]));
                 out[p * n + q] = o;
                 if (q != p) out[q * n + p] = o;
             }
@@ -266,7 +277,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
             const int64_t q = q0 + j;
             if (q <= p && q < n) {
                 const float o = static_cast<float>(
-                    0.5 * (static_cast<double>(ep.x32[p * n + q]) + up * static_cast<double>(ep.acc_scale * v[j])));
+                    0.5 * (static_cast<double>(ep.x32[p * n + q]) + up * static_cast<double>(acc_scale * v[j])));
                 ep.out32[p * n + q] = o;
                 if (q != p) ep.out32[q * n + p] = o;
             }
@@ -276,7 +287,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
     if (ep.skip_pad && (p0 >= ti.blk.n || q0 >= ti.blk.n)) return;  // padding run (warp-uniform)
     const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) v[j] *= ep.acc_scale;
+    for (int j = 0; j < 32; ++j) v[j] *= acc_scale;
     if (ep.kind == EPI_STEP) {
 #pragma unroll
         for (int g = 0; g < 4; ++g) {

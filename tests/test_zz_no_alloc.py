@@ -1,13 +1,15 @@
 """psdgb_composite_static: the composite filter without any device allocation.
 
 Callers that cannot allocate device memory — a solver that has reserved the
-GPU's memory and hands out only its own buffers, a real-time loop that may not
-wait on or fail in the allocator, code running under stream capture — use
-psdgb_composite_static, whose scratch is a device array the library reserves
-when it is loaded.  This file checks, through the C ABI, that two calls in a
-row match psdgb_composite (which takes its scratch from a workspace) within
-the FP32-class tolerance of the other GPU tests (3e-5 relative Frobenius),
-and that sizes beyond its 512 limit are refused with a clear error.
+GPU's memory and hands out only its own buffers, or a real-time loop that may
+not wait on or fail in the allocator — use psdgb_composite_static, whose
+scratch is a file-scope device array in the library's CUDA module.  This file
+checks, through the C ABI, that two calls in a row match psdgb_composite
+(which takes its scratch from a workspace) within the FP32-class tolerance of
+the other GPU tests (3e-5 relative Frobenius), that a call leaves the device's
+free memory unchanged (with the library's cached workspace released first, so
+a hidden use of it would show), and that sizes beyond its 512 limit are
+refused with a clear error.
 
 It is named to be collected last, so a run that stops at the first failure
 has already run every other test; it passes alone in a fresh process too.
@@ -50,11 +52,19 @@ def test_static_matches_workspace_entry_point_twice(precision_name, n):
     _capi.check(lib.psdgb_composite(prec, sched, ctypes.c_void_p(ref.data_ptr()), n, None, 0, stream),
                 "psdgb_composite")
     want = ref.cpu().numpy()
+    # Drop the cached workspace psdgb_composite just filled: the static calls
+    # must not use (or re-create) it.
+    _capi.check(lib.psdgb_release_workspace(), "psdgb_release_workspace")
 
-    for _ in range(2):  # two calls in a row share (and reuse) the static scratch
-        t = torch.from_numpy(np.ascontiguousarray(x.T)).cuda()
+    bufs = [torch.from_numpy(np.ascontiguousarray(x.T)).cuda() for _ in range(2)]
+    torch.cuda.synchronize()
+    for i, t in enumerate(bufs):  # two calls in a row share (and reuse) the static scratch
+        free_before = torch.cuda.mem_get_info()[0]
         st = lib.psdgb_composite_static(prec, sched, ctypes.c_void_p(t.data_ptr()), n, stream)
+        free_after = torch.cuda.mem_get_info()[0]
         _capi.check(st, "psdgb_composite_static")
+        if i == 1:  # the first call on a device may load the module that holds the array
+            assert free_after == free_before, (free_before, free_after)
         got = t.cpu().numpy()
         assert np.all(np.isfinite(got))
         assert _rel(got, want) <= TOL
