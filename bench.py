@@ -65,6 +65,7 @@ def parse_args():
     ap.add_argument("--no-batch", action="store_true", help="skip the block-diagonal batch session")
     ap.add_argument("--only-batch", action="store_true", help="run only the block-diagonal batch session")
     ap.add_argument("--only-configs", action="store_true", help="run only the n=1024 and n=16384 sessions")
+    ap.add_argument("--only-serve", action="store_true", help="run only the serving sessions")
     ap.add_argument("--no-configs", action="store_true", help="skip the n=1024 and n=16384 sessions")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
@@ -242,7 +243,8 @@ def dense_equiv_flops(n: int, steps: int) -> float:
 # ---------------------------------------------------------------------------
 
 def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 4096), n_streams: int = 64,
-                  seed: int = 0, max_slots: int = 16, check_error: bool = False, admission: str = "fifo") -> dict:
+                  seed: int = 0, max_slots: int = 16, check_error: bool = False, admission: str = "fifo",
+                  priority_n: int = 0, reserve_sms: int = 0) -> dict:
     """Closed-loop ADMM streams: stream k (n = sizes[k % 4]) waits an
     exponential think time (mean n_streams / offered_rate), perturbs its
     matrix by 1e-2 (E + E^T)/2, submits it, and waits for the projection
@@ -268,7 +270,8 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
     torch.cuda.synchronize()
     mean_think = n_streams / offered_rate
     lat, lat_by_n, gpu_ms = [], {n: [] for n in sizes}, []
-    with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10, admission=admission) as srv:
+    with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10, admission=admission,
+                priority_n=priority_n, reserve_sms=reserve_sms) as srv:
         # warm the per-(slot, n) graphs outside the measured window
         for k in range(min(n_streams, 2 * len(sizes))):
             srv.submit(k, mats[k], outs[k])
@@ -315,7 +318,8 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
                 errs[ns[k]] = psd.rel_frobenius(outs[k], ref)
             err = errs
     a = np.array(lat) * 1e3
-    return {"offered_req_s": offered_rate, "admission": admission, "throughput_req_s": completed / wall,
+    return {"offered_req_s": offered_rate, "admission": admission, "priority_n": priority_n,
+            "reserve_sms": reserve_sms, "throughput_req_s": completed / wall,
             "completed": completed,
             "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
             "p99_ms": float(np.percentile(a, 99)) if len(a) else None,
@@ -610,6 +614,18 @@ def cpu_evd_projection_time(xs) -> float:
 # arms
 # ---------------------------------------------------------------------------
 
+def serving_sessions(args) -> dict:
+    sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
+    sessions += [serve_session(r, args.serve_seconds, admission="shortest_first") for r in (500.0, 2000.0)]
+    # Small requests (n <= 1024) on high-priority streams, 16 SMs kept free of the n = 4096 products.
+    sessions += [serve_session(2000.0, args.serve_seconds, admission=a, priority_n=1024, reserve_sms=16)
+                 for a in ("fifo", "shortest_first")]
+    return {"workload": "64 closed-loop ADMM-like streams, n uniform over {64,256,1024,4096} (16 streams each), "
+                        "next matrix = previous + 1e-2 (E+E^T)/2, exponential think time for the offered rate; "
+                        "fp16x3, warm-started Lanczos (10 steps), 16 slots, CUDA-graph replay",
+            "sessions": sessions}
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -782,13 +798,7 @@ def run_ours(args, rank, world):
         out["deflation"] = deflation_session()
 
     if not args.no_serve:
-        sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
-        sessions += [serve_session(r, args.serve_seconds, admission="shortest_first") for r in (500.0, 2000.0)]
-        out["serving"] = {
-            "workload": "64 closed-loop ADMM-like streams, n uniform over {64,256,1024,4096} (16 streams each), "
-                        "next matrix = previous + 1e-2 (E+E^T)/2, exponential think time for the offered rate; "
-                        "fp16x3, warm-started Lanczos (10 steps), 16 slots, CUDA-graph replay",
-            "sessions": sessions}
+        out["serving"] = serving_sessions(args)
 
     if world == 1 and not args.no_cpu_baseline:
         xs = X.cpu().numpy()
@@ -879,6 +889,9 @@ def main():
     rank, world = dist_setup()
     if args.only_batch:
         print(json.dumps({"batched": batched_session(count=args.batch_count)}))
+        return
+    if args.only_serve:
+        print(json.dumps({"serving": serving_sessions(args)}))
         return
     if args.only_configs:
         print(json.dumps({"config1": config1_session(), "config3": config3_session(),

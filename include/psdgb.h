@@ -243,6 +243,9 @@ typedef struct psdgb_server_config {
                                  that does not fit the budget yet is skipped); PSDGB_ADMIT_SHORTEST_FIRST:
                                  among each key's oldest queued request, the smallest n starts first
                                  (ties by submission).  Both keep every key's requests in order. */
+    int64_t priority_n;       /* > 0: requests with n <= priority_n run on high-priority streams and the
+                                 persistent kernels of larger requests leave reserve_sms SMs free; 0: off */
+    int reserve_sms;          /* SMs kept free of large requests' persistent kernels (with priority_n) */
 } psdgb_server_config;
 enum { PSDGB_ADMIT_FIFO = 0, PSDGB_ADMIT_SHORTEST_FIRST = 1 };
 

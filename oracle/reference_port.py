@@ -338,7 +338,7 @@ def composite_split_model(X: np.ndarray, precision: str = "fp16x3", schedule: st
     """What this library's kernels compute for composite on X with scale up:
     operands split into terms, products summed over the precision's term
     pairs (accumulated here in FP64, on the GPU in FP32; one-term modes take
-    the symmetric part of the third product of each step), the step combination
+    the symmetric parts of the second and third products of each step), the step combination
     a*A + b*A3 + c*A3*A2 in FP32 on the stored values, and the final
     0.5 * (X + up * (Xs*A + A*Xs)/2) in FP64."""
     fmt, _, prods = PRECISION_MODEL[precision]
@@ -348,8 +348,8 @@ def composite_split_model(X: np.ndarray, precision: str = "fp16x3", schedule: st
     A_t = split_terms(Xs32, fmt)
     for a, b, c in schedule_coefficients(schedule):
         A2_t = split_terms(_product(A_t, A_t, prods), fmt)
-        A3_t = split_terms(_product(A2_t, A_t, prods), fmt)
-        acc = _product(A3_t, A2_t, prods, dual=one_term)  # one-term modes: symmetric part of A3*A2
+        A3_t = split_terms(_product(A2_t, A_t, prods, dual=one_term), fmt)  # one-term modes: symmetric parts
+        acc = _product(A3_t, A2_t, prods, dual=one_term)
         A_new = np.float32(c) * acc + (np.float32(b) * _stored(A3_t) + np.float32(a) * _stored(A_t))
         A_t = split_terms(A_new.astype(np.float32), fmt)
     PA = _product(split_terms(Xs32, fmt), A_t, prods, dual=True).astype(np.float64)

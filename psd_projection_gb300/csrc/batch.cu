@@ -502,6 +502,10 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         EpiParams e2 = base();
         e2.kind = EPI_STORE;
         e2.out = b->A3;
+        if (dual_step) {  // one-term precisions: symmetric part, as for a single matrix (composite.cu)
+            e2.dual = 1;
+            e2.acc_scale = 0.5f;
+        }
         PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, e2, gw, b->num_tiles,
                                 0, s));
         EpiParams e3 = base();

@@ -83,6 +83,8 @@ Handles& handles_for_device(int dev) {
 
 }  // namespace
 
+thread_local int g_sm_cap = 0;
+
 void set_error(const std::string& msg) { g_last_error = msg; }
 
 psdgb_status cuda_fail(cudaError_t e, const char* what) {

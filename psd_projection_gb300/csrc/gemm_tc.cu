@@ -265,7 +265,7 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
         }
     }
     if (num_tiles <= 0) return PSDGB_OK;
-    int g = grid > 0 ? grid : ds->sm_count;
+    int g = grid > 0 ? grid : sm_budget(ds);
     if (g > num_tiles) g = static_cast<int>(num_tiles);
     kern<<<static_cast<unsigned>(g), 64 + 32 * EW, Cfg::SMEM_BYTES, s>>>(tm, ep, gw, static_cast<int>(num_tiles),
                                                                     ds->d_error);

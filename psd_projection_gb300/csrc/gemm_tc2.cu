@@ -339,7 +339,8 @@ psdgb_status launch_pair(DeviceState* ds, const SplitMat& P, const SplitMat& Q, 
     }
     const int64_t num_pairs = pair_tile_count(np / BM);
     if (num_pairs <= 0) return PSDGB_OK;
-    const int clusters = num_pairs < max_clusters ? static_cast<int>(num_pairs) : max_clusters;
+    int clusters = num_pairs < max_clusters ? static_cast<int>(num_pairs) : max_clusters;
+    if (clusters > sm_budget(ds) / 2) clusters = sm_budget(ds) / 2 > 0 ? sm_budget(ds) / 2 : 1;
     kern<<<static_cast<unsigned>(2 * clusters), THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, g_tile_group_rows,
                                                                              static_cast<int>(num_pairs), ds->d_error);
     count_launch();

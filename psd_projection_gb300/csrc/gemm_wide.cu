@@ -367,7 +367,7 @@ psdgb_status launch_wide(DeviceState* ds, const SplitMat& P, const SplitMat& Q, 
     }
     const int64_t num_tiles = wide_tile_count(np / BM);
     if (num_tiles <= 0) return PSDGB_OK;
-    const int grid = num_tiles < ds->sm_count ? static_cast<int>(num_tiles) : ds->sm_count;
+    const int grid = num_tiles < sm_budget(ds) ? static_cast<int>(num_tiles) : sm_budget(ds);
     kern<<<static_cast<unsigned>(grid), W_THREADS, Cfg::SMEM_BYTES, s>>>(tm, ep, g_tile_group_rows,
                                                                       static_cast<int>(num_tiles), ds->d_error);
     count_launch();

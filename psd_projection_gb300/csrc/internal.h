@@ -49,6 +49,13 @@ struct DeviceState {
     size_t stage2_bytes = 0;
 };
 psdgb_status device_state(DeviceState** out);
+// Upper bound on the CTAs (one per SM) of the persistent kernels this thread
+// launches, 0 for every SM: the request loop caps its large requests' kernels
+// so that some SMs stay free for small requests (csrc/serve.cu).
+extern thread_local int g_sm_cap;
+inline int sm_budget(const DeviceState* ds) {
+    return (g_sm_cap > 0 && g_sm_cap < ds->sm_count) ? g_sm_cap : ds->sm_count;
+}
 // Synchronise the stream and turn a device error word into a status.
 psdgb_status finish(DeviceState* ds, cudaStream_t stream);
 

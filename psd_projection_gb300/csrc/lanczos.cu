@@ -890,10 +890,10 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
     const int nqdot = static_cast<int>((n + 31) / 32);
     const int nnorm = static_cast<int>((n + UPB_ROWS - 1) / UPB_ROWS);
     for (int64_t k = 0; k < m; ++k) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, ds->sm_count, s, sv));  // u = A q
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, stopped, sm_budget(ds), s, sv));  // u = A q
         if (sv.on) {
             // w = A^T u with the q.w partials; the update over nnorm blocks.
-            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv, P.q, P.qdot));
+            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, sm_budget(ds), s, sv, P.q, P.qdot));
             lz_upd_axpy_kernel<<<static_cast<unsigned>(nnorm), UPB_THREADS, 0, s>>>(
                 n, static_cast<int>(k), P.st, P.alpha, P.q, P.w, P.vold, P.qdot, nqdot, P.norm);
             count_launch();
@@ -903,7 +903,7 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
             count_launch();
             PSDGB_CUDA_TRY(cudaGetLastError());
         } else {
-            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, ds->sm_count, s, sv));  // w = A^T u
+            PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.w, nullptr, stopped, sm_budget(ds), s, sv));  // w = A^T u
             lz_update_kernel<<<1, UPD_THREADS, 0, s>>>(n, m, static_cast<int>(k), tol, P.st, P.alpha, P.beta, P.q,
                                                        P.w, P.vold, P.V, P.q32);
             count_launch();
@@ -926,10 +926,10 @@ psdgb_status lanczos_bound_async(DeviceState* ds, const float* a32, int64_t n, i
     }
     const int* no_ritz = &P.st->no_ritz;
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, no_ritz, ds->sm_count, s, sv));  // A y
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.ry, nullptr, no_ritz, ds->sm_count, s, sv));   // A^T A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, nullptr, P.u32, no_ritz, sm_budget(ds), s, sv));  // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.u32, P.ry, nullptr, no_ritz, sm_budget(ds), s, sv));   // A^T A y
     } else {
-        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, P.ry, nullptr, no_ritz, ds->sm_count, s, sv));   // A y
+        PSDGB_CUDA_TRY(matvec(a32, n, ld, P.q32, P.ry, nullptr, no_ritz, sm_budget(ds), s, sv));   // A y
     }
     lz_resid_kernel<<<1, 1024, 0, s>>>(n, P.ry, P.y, P.st);
     count_launch();

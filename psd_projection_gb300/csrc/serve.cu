@@ -21,7 +21,13 @@
 //     warm_max_iter steps instead of max_iter);
 //   * CUDA graphs — with use_graphs, the whole projection of a given n on a
 //     slot is captured once and replayed (a few launches per request instead
-//     of ~100).
+//     of ~100);
+//   * small requests first on the device — with priority_n > 0, requests of
+//     n <= priority_n run on high-priority streams, and the persistent
+//     kernels of larger requests are capped at (SMs - reserve_sms) CTAs, so
+//     reserve_sms SMs are always free of them: a small request's short kernels
+//     start at once instead of waiting for a large product kernel, which holds
+//     every SM it was given until it ends, to drain.
 //
 // Every request's result depends only on its input and its key's previous
 // request: kernels are deterministic and a slot's buffers are private while
@@ -66,7 +72,8 @@ struct KeyState {
 };
 
 struct Slot {
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;   // the stream of the current (or last) request: one of the two below
+    cudaStream_t streams[2] = {nullptr, nullptr};  // [0] lowest priority, [1] highest
     cudaEvent_t ev_start = nullptr, ev_end = nullptr;
     int64_t cap_n = 0;          // buffers sized for this n
     size_t bytes = 0;           // device bytes held
@@ -161,10 +168,31 @@ psdgb_status enqueue_projection(psdgb_server* s, Slot& sl, int64_t n, bool warm)
                                             sl.lz_bytes, sl.stream);
 }
 
+// Small requests (n <= priority_n) go to the slot's high-priority stream;
+// large ones to its low-priority stream with their persistent kernels capped.
+bool is_small(const psdgb_server_config& c, int64_t n) { return c.priority_n > 0 && n <= c.priority_n; }
+
+struct SmCapScope {  // caps this thread's persistent kernels while a large request is enqueued
+    int old;
+    explicit SmCapScope(int cap) : old(psdgb::g_sm_cap) { psdgb::g_sm_cap = cap; }
+    ~SmCapScope() { psdgb::g_sm_cap = old; }
+};
+
+int large_request_cap(const psdgb_server_config& c) {
+    if (c.priority_n <= 0 || c.reserve_sms <= 0) return 0;
+    psdgb::DeviceState* ds = nullptr;
+    if (psdgb::device_state(&ds) != PSDGB_OK) return 0;
+    const int cap = ds->sm_count - c.reserve_sms;
+    return cap >= 2 ? cap : 2;
+}
+
 psdgb_status launch_request(psdgb_server* s, Slot& sl, const Request& r) {
     KeyState& ks = s->keys[r.key];
     const int64_t n = r.n;
     const bool warm = ks.valid && ks.n == n;
+    const bool small = is_small(s->cfg, n);
+    sl.stream = sl.streams[small ? 1 : 0];
+    SmCapScope cap(small ? 0 : large_request_cap(s->cfg));
     PSDGB_CUDA_TRY(cudaEventRecord(sl.ev_start, sl.stream));
     PSDGB_CUDA_TRY(cudaMemcpyAsync(sl.mat, r.d_in, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, sl.stream));
     if (warm) PSDGB_CUDA_TRY(cudaMemcpyAsync(sl.warm, ks.ritz, sizeof(double) * n, cudaMemcpyDeviceToDevice, sl.stream));
@@ -231,6 +259,8 @@ psdgb_status try_start(psdgb_server* s, const Request& r, bool* started, bool* n
         }
         const size_t need = slot_bytes(s->cfg, r.n) + up256(sizeof(double) * r.n);
         if (s->used_bytes - spare->bytes + need > s->cfg.hbm_budget_bytes) return PSDGB_OK;  // not yet
+        // Re-size on the stream the request will run on (stream-ordered allocation).
+        spare->stream = spare->streams[is_small(s->cfg, r.n) ? 1 : 0];
         PSDGB_TRY(slot_resize(s, *spare, r.n));
         pick = spare;
     }
@@ -300,6 +330,7 @@ double psdgb_clock_seconds(void) { return now_s(); }
 
 psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** out) {
     if (!cfg || !out || cfg->max_slots <= 0 || cfg->max_slots > 256 || cfg->max_iter < 0 || cfg->warm_max_iter < 0 ||
+        cfg->priority_n < 0 || cfg->reserve_sms < 0 ||
         (cfg->admission != PSDGB_ADMIT_FIFO && cfg->admission != PSDGB_ADMIT_SHORTEST_FIRST)) {
         set_error("psdgb_server_create: bad configuration");
         return PSDGB_ERR_INVALID_ARGUMENT;
@@ -324,7 +355,11 @@ psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** 
     s->cfg = *cfg;
     for (int i = 0; i < cfg->max_slots; ++i) {
         auto sl = std::make_unique<Slot>();
-        PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking));
+        int least = 0, greatest = 0;
+        PSDGB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        PSDGB_CUDA_TRY(cudaStreamCreateWithPriority(&sl->streams[0], cudaStreamNonBlocking, least));
+        PSDGB_CUDA_TRY(cudaStreamCreateWithPriority(&sl->streams[1], cudaStreamNonBlocking, greatest));
+        sl->stream = sl->streams[0];
         PSDGB_CUDA_TRY(cudaEventCreate(&sl->ev_start));
         PSDGB_CUDA_TRY(cudaEventCreate(&sl->ev_end));
         s->slots.push_back(std::move(sl));
@@ -336,11 +371,14 @@ psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** 
 psdgb_status psdgb_server_destroy(psdgb_server* s) {
     if (!s) return PSDGB_OK;
     for (auto& sl : s->slots) {
-        cudaStreamSynchronize(sl->stream);
+        cudaStreamSynchronize(sl->streams[0]);
+        cudaStreamSynchronize(sl->streams[1]);
         slot_release(s, *sl);
+        cudaStreamSynchronize(sl->stream);
         cudaEventDestroy(sl->ev_start);
         cudaEventDestroy(sl->ev_end);
-        cudaStreamDestroy(sl->stream);
+        cudaStreamDestroy(sl->streams[0]);
+        cudaStreamDestroy(sl->streams[1]);
     }
     cudaDeviceSynchronize();
     for (auto& kv : s->keys)

@@ -8,9 +8,10 @@ to free, composite_FP32 with a workspace of the reference's documented size
 (3 n^2 floats), and a failing call (printed, then execution continues).
 
 Tolerances (relative Frobenius against the host FP64 dsyevd projection):
-1e-4 for the FP32-class methods and eig_FP32_psd, 1e-3 for composite_FP16
-(the reference's FP16 bar, test/composite_FP16_test.hpp:129), 1e-10 for
-eig_FP64_psd; the Lanczos bounds must bracket ||A||_2 = 7.0890 as in
+1e-4 for the FP32-class methods and eig_FP32_psd; for composite_FP16, 1.05x
+the error of the oracle's restatement of the reference's FP16 method on the
+same input (test_gpu_configs.py explains the 5 %); 1e-10 for eig_FP64_psd;
+the Lanczos bounds must bracket ||A||_2 = 7.0890 as in
 test/lanczos_test.hpp:40-41 (up to the rounding of that figure).
 """
 import json
@@ -65,11 +66,14 @@ def run_caller(tmp_path_factory):
     return inputs, lines, Outputs(), r.stdout
 
 
-@pytest.mark.parametrize("method,tol", [("composite_FP32_auto_scale", 1e-4), ("composite_FP16_auto_scale", 1e-3),
+@pytest.mark.parametrize("method,tol", [("composite_FP32_auto_scale", 1e-4), ("composite_FP16_auto_scale", None),
                                         ("composite_FP32_emulated_auto_scale", 1e-4)])
 def test_auto_scaled_methods(run_caller, method, tol):
     inputs, lines, out, _ = run_caller
     proj, _ = rp.eig_psd(inputs["x300"])
+    if tol is None:  # the reference FP16 method's own error level on this input
+        ref, _ = rp.composite_auto_scale(inputs["x300"], "fp16")
+        tol = 1.05 * rp.rel_frobenius(ref, proj)
     assert rp.rel_frobenius(out(method, 300), proj) <= tol
 
 

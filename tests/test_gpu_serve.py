@@ -32,14 +32,16 @@ def _streams(sizes, steps, seed=0):
     return seqs
 
 
-def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_iter=10, admission="fifo"):
+def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_iter=10, admission="fifo",
+           priority_n=0, reserve_sms=0):
     import torch
 
     from psd_projection_gb300.serve import Server
 
     outs = {}
     with Server(hbm_budget_bytes=budget, max_slots=max_slots, use_graphs=use_graphs,
-                warm_max_iter=warm_max_iter, admission=admission) as srv:
+                warm_max_iter=warm_max_iter, admission=admission, priority_n=priority_n,
+                reserve_sms=reserve_sms) as srv:
         ins = {}
         order = []
         steps = len(seqs[0])
@@ -131,3 +133,15 @@ def test_shortest_first_admission_keeps_results_and_key_order():
     assert order[1:] == sorted(order[1:])
     with pytest.raises(ValueError):
         Server(admission="lifo")
+
+
+def test_priority_streams_and_sm_reserve_keep_results():
+    """Small requests on high-priority streams and large requests' persistent
+    kernels capped below the SM count: every result is still the one-at-a-time
+    result bit for bit (each tile and matvec partial is computed by one CTA in
+    a fixed order, whatever the grid)."""
+    seqs = _streams([64, 1024, 256, 2100, 64], steps=2, seed=5)
+    alone, _ = _serve(seqs, max_slots=1, together=False)
+    prio, _ = _serve(seqs, max_slots=6, together=True, priority_n=256, reserve_sms=24)
+    for kt in alone:
+        assert np.array_equal(alone[kt], prio[kt]), kt
