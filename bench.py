@@ -66,6 +66,9 @@ def parse_args():
     ap.add_argument("--only-batch", action="store_true", help="run only the block-diagonal batch session")
     ap.add_argument("--only-configs", action="store_true", help="run only the n=1024 and n=16384 sessions")
     ap.add_argument("--only-serve", action="store_true", help="run only the serving sessions")
+    ap.add_argument("--profile-case", nargs=2, metavar=("KIND", "SIZE"),
+                    help="small fixed workloads for ncu captures: 'single N' (two auto-scaled fp16x3 projections of "
+                         "one n=N Gaussian matrix) or 'batch COUNT' (two projections of a COUNT-block batch)")
     ap.add_argument("--no-configs", action="store_true", help="skip the n=1024 and n=16384 sessions")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--serve-seconds", type=float, default=2.0)
@@ -414,14 +417,18 @@ def config3_session(n: int = 16384, seed: int = 3) -> dict:
     timed("bf16x9", lambda t: psd.composite(t, psd.PRECISIONS["bf16x9"], P32))
     timed("bf16_bulk_only", lambda t: psd.composite(t, psd.PRECISIONS["bf16"], P16))
     timed("fp16_bulk_only", lambda t: psd.composite(t, psd.PRECISIONS["fp16"], P16))
+    timed("fp8_bulk_only", lambda t: psd.composite(t, psd.PREC_FP8, psd.SCHEDULE_FP8))
     for r in (1, 2):
         timed(f"bf16_bulk+{r}x_bf16x9_refine", lambda t, r=r: psd.composite_mixed(t, "bf16", "bf16x9", r))
         timed(f"fp16_bulk+{r}x_fp16x3_refine", lambda t, r=r: psd.composite_mixed(t, "fp16", "fp16x3", r))
+        timed(f"fp8_bulk+{r}x_fp16x3_refine", lambda t, r=r: psd.composite_mixed(t, "fp8", "fp16x3", r))
     return {"workload": f"n={n} precision stress: 10% |lambda|<1e-3, 60% U[-1,-1e-3], 30% U[1e-3,10], "
-                        "Q=QR(N(0,1)) seed 3, FP32 storage; bulk = one-term products on the FP16 schedule, "
+                        "Q=QR(N(0,1)) seed 3, FP32 storage; bulk = one-term products (FP16 / BF16 on the FP16 "
+                        "schedule, FP8 E4M3 on the FP8 schedule: the FP16 table with safety factor 1.5), "
                         "refinement = the FP32 table's final quintic in split precision",
             "setup_s": setup_s, "runs": runs,
-            "note": "FP8 e4m3 bulk is not built; BF16 and FP16 one-term bulks stand in for it"}
+            "note": "FP8 products: tcgen05.mma kind::f8f6f4 on 128x128 tiles, E4M3 operand copies beside the "
+                    "FP16 pair the refinement reads"}
 
 
 # ---------------------------------------------------------------------------
@@ -613,6 +620,43 @@ def cpu_evd_projection_time(xs) -> float:
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
+
+def profile_case(kind: str, size: str) -> None:
+    """Fixed small workloads to run under ncu (no timing, no oracle)."""
+    import numpy as np
+    import torch
+
+    import psd_projection_gb300 as psd
+
+    n = int(size)
+    if kind == "single":
+        g = torch.Generator(device="cuda")
+        g.manual_seed(0)
+        G = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")
+        X = ((0.5 / n ** 0.5) * (G + G.T)).float().double().contiguous()
+        del G
+        for _ in range(2):
+            psd.composite(X.clone())
+    elif kind == "batch":
+        from psd_projection_gb300.batch import BatchPlan
+
+        rng = np.random.default_rng(0)
+        sizes = [int(round(v)) for v in np.exp(rng.uniform(np.log(16), np.log(512), n))]
+        offs = np.concatenate([[0], np.cumsum([m * m for m in sizes])])
+        g = torch.Generator(device="cuda")
+        g.manual_seed(0)
+        d = torch.empty(int(offs[-1]), dtype=torch.float64, device="cuda")
+        for b, m in enumerate(sizes):
+            G = torch.randn((m, m), generator=g, dtype=torch.float64, device="cuda")
+            d[offs[b]:offs[b + 1]].copy_((0.5 * (G + G.T)).float().double().reshape(-1))
+        plan = BatchPlan(sizes)
+        for _ in range(2):
+            plan.project(d.clone())
+    else:
+        raise SystemExit("--profile-case KIND is 'single' or 'batch'")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": kind, "size": n}))
+
 
 def serving_sessions(args) -> dict:
     sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
@@ -889,6 +933,9 @@ def main():
     rank, world = dist_setup()
     if args.only_batch:
         print(json.dumps({"batched": batched_session(count=args.batch_count)}))
+        return
+    if args.profile_case:
+        profile_case(*args.profile_case)
         return
     if args.only_serve:
         print(json.dumps({"serving": serving_sessions(args)}))

@@ -59,15 +59,20 @@ typedef enum psdgb_precision {
     PSDGB_PREC_FP16X3 = 3,    /* FP16 hi/lo split, products hi*hi + hi*lo + lo*hi */
     PSDGB_PREC_BF16X3 = 4,    /* BF16 hi/lo split, 3 products */
     PSDGB_PREC_BF16X6 = 5,    /* BF16 3-term split, the 6 products of order <= 2 */
-    PSDGB_PREC_BF16X9 = 6     /* BF16 3-term split, all 9 products (FP32 emulation) */
+    PSDGB_PREC_BF16X9 = 6,    /* BF16 3-term split, all 9 products (FP32 emulation) */
+    PSDGB_PREC_FP8 = 7        /* one FP8 E4M3 term per operand, tcgen05 kind::f8f6f4, FP32 accumulate;
+                                 the stored iterate keeps the FP16 hi/lo pair (FP16 schedule only) */
 } psdgb_precision;
 
 /* Polynomial schedule of the sign filter. */
 typedef enum psdgb_schedule {
     PSDGB_SCHEDULE_FP32 = 0,  /* 10 quintic steps, safety factor 1.001 on the first 8
                                  (src/composite_FP32.cu:73-99) */
-    PSDGB_SCHEDULE_FP16 = 1   /* 7 quintic steps, safety factor 1.01 on every step
+    PSDGB_SCHEDULE_FP16 = 1,  /* 7 quintic steps, safety factor 1.01 on every step
                                  (src/composite_FP16.cu:93-113) */
+    PSDGB_SCHEDULE_FP8 = 2    /* the FP16 table's 7 steps with safety factor 1.5 on every step: E4M3
+                                 operand rounding (2^-4) pushes eigenvalues well past 1.01 (no
+                                 counterpart in the reference; the schedule of PSDGB_PREC_FP8) */
 } psdgb_schedule;
 
 /* Residual formula of the Lanczos upper bound. */

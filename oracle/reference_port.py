@@ -170,11 +170,13 @@ def approximate_two_norm(A: np.ndarray, max_iter: int = 20, tol: float = 1e-10, 
 def schedule_coefficients(schedule: str = "fp32") -> list[tuple[np.float32, np.float32, np.float32]]:
     """Per-step (a, b, c) after the safety scaling, in FP32 arithmetic like the
     reference: s = 1.001 on steps 0-7 of the FP32 table
-    (src/composite_FP32.cu:86-99), s = 1.01 on every FP16 step (src/composite_FP16.cu:103-113)."""
+    (src/composite_FP32.cu:86-99), s = 1.01 on every FP16 step (src/composite_FP16.cu:103-113).
+    "fp8" (this library's FP8 schedule, no reference counterpart): the FP16
+    table with s = 1.5 on every step."""
     f = np.float32
     out = []
-    if schedule == "fp16":
-        s = f(1.01)
+    if schedule in ("fp16", "fp8"):
+        s = f(1.5) if schedule == "fp8" else f(1.01)
         for a, b, c in COEFF_FP16:
             a, b, c = f(a), f(b), f(c)
             out.append((f(a / s), f(b / (s * s * s)), f(c / (s * s * s * s * s))))
@@ -279,11 +281,30 @@ PRECISION_MODEL = {
     "bf16x3": ("bf16", 3, [(0, 0), (0, 1), (1, 0)]),
     "bf16x6": ("bf16", 3, [(0, 0), (0, 1), (1, 0), (0, 2), (2, 0), (1, 1)]),
     "bf16x9": ("bf16", 3, [(i, j) for i in range(3) for j in range(3)]),
+    # FP8: the products read an E4M3 copy (term index 2 of the "f16q8" format),
+    # the stored value is the FP16 pair.
+    "fp8": ("f16q8", 3, [(2, 2)]),
 }
 
 
 # Factor of the FP16 operand terms (psd_projection_gb300/csrc/common.cuh, kF16Scale).
 F16_SCALE = np.float32(4096.0)
+# Factor of the E4M3 plane (common.cuh, kE4M3Scale).
+E4M3_SCALE = np.float32(128.0)
+
+
+def to_e4m3(x: np.ndarray) -> np.ndarray:
+    """Round FP32 to FP8 E4M3 (OCP: 4 exponent bits, bias 7, 3 mantissa bits,
+    subnormals below 2^-6, largest finite 448; round to nearest even,
+    saturating at +-448), returned as FP32."""
+    x = np.asarray(x, dtype=np.float64)
+    a = np.abs(x)
+    e = np.floor(np.log2(np.where(a > 0, a, 1.0)))
+    e = np.maximum(e, -6.0)                      # subnormal spacing 2^-9 below 2^-6
+    q = 2.0 ** (e - 3.0)                         # spacing of the 3-bit significand at exponent e
+    r = np.round(a / q) * q                      # numpy rounds halves to even
+    r = np.minimum(r, 448.0)
+    return (np.sign(x) * r).astype(np.float32)
 
 
 def _to_bf16(x: np.ndarray) -> np.ndarray:
@@ -298,6 +319,10 @@ def split_terms(x32: np.ndarray, fmt: str) -> list[np.ndarray]:
     x32 = np.asarray(x32, dtype=np.float32)
     if fmt == "f32":
         return [x32]
+    if fmt == "f16q8":
+        hi, lo = split_terms(x32, "f16")
+        q = (to_e4m3((x32 * E4M3_SCALE).astype(np.float32)) / E4M3_SCALE).astype(np.float32)
+        return [hi, lo, q]
     if fmt == "f16":
         # The kernels split v * 2^12 (F16_SCALE) so that the low term stays a
         # normal FP16 number, and take the factor out of every product and
@@ -313,7 +338,9 @@ def split_terms(x32: np.ndarray, fmt: str) -> list[np.ndarray]:
     return [b0, b1, b2]
 
 
-def _stored(terms: list[np.ndarray]) -> np.ndarray:
+def _stored(terms: list[np.ndarray], fmt: str = "") -> np.ndarray:
+    if fmt == "f16q8":
+        terms = terms[:2]  # the stored value is the FP16 pair
     s = np.zeros_like(terms[0], dtype=np.float32)
     for t in reversed(terms):
         s = (s + t).astype(np.float32)
@@ -350,7 +377,7 @@ def composite_split_model(X: np.ndarray, precision: str = "fp16x3", schedule: st
         A2_t = split_terms(_product(A_t, A_t, prods), fmt)
         A3_t = split_terms(_product(A2_t, A_t, prods, dual=one_term), fmt)  # one-term modes: symmetric parts
         acc = _product(A3_t, A2_t, prods, dual=one_term)
-        A_new = np.float32(c) * acc + (np.float32(b) * _stored(A3_t) + np.float32(a) * _stored(A_t))
+        A_new = np.float32(c) * acc + (np.float32(b) * _stored(A3_t, fmt) + np.float32(a) * _stored(A_t, fmt))
         A_t = split_terms(A_new.astype(np.float32), fmt)
     PA = _product(split_terms(Xs32, fmt), A_t, prods, dual=True).astype(np.float64)
     out = 0.5 * (X + up * PA)   # symmetric part of Xs*A, one dual product on the GPU

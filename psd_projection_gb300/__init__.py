@@ -29,9 +29,9 @@ from __future__ import annotations
 import ctypes
 
 from . import _capi
-from ._capi import (DEFAULT_SEED, PREC_BF16, PREC_BF16X3, PREC_BF16X6, PREC_BF16X9, PREC_FP16, PREC_FP16X3,
-                    PREC_FP32_SIMT, PRECISIONS, RESIDUAL_EXACT, RESIDUAL_REFERENCE, SCHEDULE_FP16, SCHEDULE_FP32,
-                    PsdgbError)
+from ._capi import (DEFAULT_SEED, PREC_BF16, PREC_BF16X3, PREC_BF16X6, PREC_BF16X9, PREC_FP8, PREC_FP16,
+                    PREC_FP16X3, PREC_FP32_SIMT, PRECISIONS, RESIDUAL_EXACT, RESIDUAL_REFERENCE, SCHEDULE_FP8,
+                    SCHEDULE_FP16, SCHEDULE_FP32, PsdgbError)
 
 __all__ = [
     "composite", "composite_mixed", "composite_FP16", "composite_FP16_auto_scale", "composite_FP32", "composite_FP32_auto_scale",
@@ -113,10 +113,13 @@ def composite(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, 
 
 
 def composite_mixed(mat, bulk: str = "bf16", refine: str = "bf16x9", refine_steps: int = 2,
-                    bulk_schedule: int = SCHEDULE_FP16, stream=None) -> None:
+                    bulk_schedule: int | None = None, stream=None) -> None:
     """Low-precision bulk (one-term products) followed by refine_steps
-    FP32-class refinement steps and reconstruction, auto-scaled, in place."""
+    FP32-class refinement steps and reconstruction, auto-scaled, in place.
+    The bulk schedule defaults to the FP8 schedule for bulk="fp8", else FP16."""
     n = _check_mat(mat)
+    if bulk_schedule is None:
+        bulk_schedule = SCHEDULE_FP8 if bulk == "fp8" else SCHEDULE_FP16
     st = _capi.lib().psdgb_composite_mixed_auto_scale(PRECISIONS[bulk], bulk_schedule, PRECISIONS[refine],
                                                       refine_steps, ctypes.c_void_p(mat.data_ptr()), n,
                                                       _stream_ptr(stream))

@@ -37,13 +37,15 @@ PREC_FP16X3 = 3
 PREC_BF16X3 = 4
 PREC_BF16X6 = 5
 PREC_BF16X9 = 6
+PREC_FP8 = 7
 PRECISIONS = {
     "fp32_simt": PREC_FP32_SIMT, "fp16": PREC_FP16, "bf16": PREC_BF16, "fp16x3": PREC_FP16X3,
-    "bf16x3": PREC_BF16X3, "bf16x6": PREC_BF16X6, "bf16x9": PREC_BF16X9,
+    "bf16x3": PREC_BF16X3, "bf16x6": PREC_BF16X6, "bf16x9": PREC_BF16X9, "fp8": PREC_FP8,
 }
 # psdgb_schedule
 SCHEDULE_FP32 = 0
 SCHEDULE_FP16 = 1
+SCHEDULE_FP8 = 2
 # psdgb_residual
 RESIDUAL_REFERENCE = 0
 RESIDUAL_EXACT = 1

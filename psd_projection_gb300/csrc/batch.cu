@@ -551,8 +551,12 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         set_error("psdgb_batch_create: the batch runs the tensor-core precisions");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
-        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+    if (precision == PSDGB_PREC_FP8) {
+        set_error("psdgb_batch_create: FP8 products run on single matrices only");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (const char* why = schedule_error(precision, schedule)) {
+        set_error(why);
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     DeviceState* ds = nullptr;

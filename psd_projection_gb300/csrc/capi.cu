@@ -339,6 +339,7 @@ const char* psdgb_precision_name(int precision) {
         case PSDGB_PREC_BF16X3: return "bf16x3";
         case PSDGB_PREC_BF16X6: return "bf16x6";
         case PSDGB_PREC_BF16X9: return "bf16x9";
+        case PSDGB_PREC_FP8: return "fp8";
         default: return nullptr;
     }
 }
@@ -451,14 +452,17 @@ psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_sched
                                               int refine_steps, double* d_mat, int64_t n, void* stream) {
     std::lock_guard<std::recursive_mutex> call(g_call_mu);
     PrecisionInfo pb{}, pr{};
-    if (!precision_info(bulk_precision, &pb) || !precision_info(refine_precision, &pr) || pb.fmt != pr.fmt ||
-        refine_steps < 0 || refine_steps > 8) {
+    // FP8 operands sit beside the FP16 pair (the F16Q8 format), so an FP8 bulk
+    // refines with fp16 / fp16x3 products on the same storage.
+    const bool fp8_bulk = bulk_precision == PSDGB_PREC_FP8;
+    if (!precision_info(bulk_precision, &pb) || !precision_info(refine_precision, &pr) ||
+        (fp8_bulk ? pr.fmt != FMT_F16 : pb.fmt != pr.fmt) || refine_steps < 0 || refine_steps > 8) {
         set_error("psdgb_composite_mixed_auto_scale: the bulk and refinement precisions must share an operand "
-                  "format (fp16 with fp16x3; bf16 with bf16x3/x6/x9) and 0 <= refine_steps <= 8");
+                  "format (fp16 or fp8 with fp16x3; bf16 with bf16x3/x6/x9) and 0 <= refine_steps <= 8");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (bulk_precision == PSDGB_PREC_BF16 && bulk_schedule != PSDGB_SCHEDULE_FP16) {
-        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+    if (const char* why = schedule_error(bulk_precision, bulk_schedule)) {
+        set_error(why);
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     if (n < 0 || (n > 0 && d_mat == nullptr)) { set_error("bad matrix"); return PSDGB_ERR_INVALID_ARGUMENT; }
@@ -468,7 +472,7 @@ psdgb_status psdgb_composite_mixed_auto_scale(int bulk_precision, int bulk_sched
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (n == 0) return PSDGB_OK;
     void *ws = nullptr, *lz = nullptr;
-    PSDGB_TRY(resolve_ws(ds, n, refine_precision, nullptr, 0, &ws));
+    PSDGB_TRY(resolve_ws(ds, n, fp8_bulk ? bulk_precision : refine_precision, nullptr, 0, &ws));
     PSDGB_TRY(resolve_lz(ds, n, 20, &lz));
     PSDGB_TRY(composite_enqueue(ds, refine_precision, bulk_schedule, d_mat, n, ws, true, 20, 1e-10, kDefaultSeed,
                                 PSDGB_RESIDUAL_REFERENCE, lz, s, nullptr, nullptr, bulk_precision, refine_steps));
@@ -703,12 +707,12 @@ psdgb_status psdgb_composite_auto_scale_deflate(int precision, int schedule, dou
                                                 double tol, double ortho_tol, uint64_t seed, void* stream) {
     std::lock_guard<std::recursive_mutex> call(g_call_mu);
     PrecisionInfo pi{};
-    if (!precision_info(precision, &pi) || (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16)) {
-        set_error("composite_auto_scale_deflate: unknown precision or schedule");
+    if (!precision_info(precision, &pi)) {
+        set_error("composite_auto_scale_deflate: unknown precision");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
-        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+    if (const char* why = schedule_error(precision, schedule)) {
+        set_error(why);
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     if (n < 0 || k < 0 || (n > 0 && d_mat == nullptr)) {
@@ -872,9 +876,9 @@ psdgb_status psdgb_composite_auto_scale_deflate_two_ends(int precision, int sche
                                                          void* stream) {
     std::lock_guard<std::recursive_mutex> call(g_call_mu);
     PrecisionInfo pi{};
-    if (!precision_info(precision, &pi) || (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) ||
-        (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16)) {
-        set_error("composite deflate: unknown precision / schedule, or one-term BF16 without the FP16 schedule");
+    if (!precision_info(precision, &pi) || schedule_error(precision, schedule)) {
+        set_error(std::string("composite deflate: ") +
+                  (precision_info(precision, &pi) ? schedule_error(precision, schedule) : "unknown precision"));
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     PSDGB_TRY(check_deflate_args(d_mat, n, k, maxiter));

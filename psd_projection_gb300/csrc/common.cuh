@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 namespace psdgb {
 
@@ -21,8 +22,11 @@ namespace psdgb {
 //   BF16 : three BF16 terms, x = b0 + b1 + b2 (Henry, Tang & Heinecke,
 //          "Leveraging the bfloat16 AI datatype for higher-precision
 //          computations", ARITH 2019).
+//   F16Q8: the F16 pair (term planes 0 and 1, the stored value) plus an FP8
+//          E4M3 plane (term 2, one byte per element) that the FP8 products
+//          read; every store writes all three.
 // ---------------------------------------------------------------------------
-enum Format : int { FMT_F32 = 0, FMT_F16 = 1, FMT_BF16 = 2 };
+enum Format : int { FMT_F32 = 0, FMT_F16 = 1, FMT_BF16 = 2, FMT_F16Q8 = 3 };
 
 struct SplitMat {
     void* term[3];   // device pointers, each Np x Np row-major (ld = Np), zero padded
@@ -42,15 +46,31 @@ struct SplitMat {
 constexpr float kF16Scale = 4096.0f;
 constexpr float kF16Unscale = 1.0f / 4096.0f;
 constexpr float kF16AccUnscale = 1.0f / 16777216.0f;
+// The E4M3 plane holds the value times 2^7: E4M3 is normal from 2^-6 and
+// saturates at 448, so entries from 1.2e-4 to 3.5 keep its 4 significant
+// bits, which covers the filter operands (|v| <= ~1.01 on the FP16
+// schedule).  Conversions saturate (satfinite), never overflow to NaN.  A
+// product of two E4M3 operands accumulates 2^14 times the true value.
+constexpr float kE4M3Scale = 128.0f;
+constexpr float kE4M3AccUnscale = 1.0f / 16384.0f;
 
 __host__ __device__ inline int format_terms(int fmt) { return fmt == FMT_F32 ? 1 : (fmt == FMT_F16 ? 2 : 3); }
-__host__ __device__ inline int format_elem_bytes(int fmt) { return fmt == FMT_F32 ? 4 : 2; }
+// Bytes of one element in term plane t.
+__host__ __device__ inline int format_plane_bytes(int fmt, int t) {
+    return fmt == FMT_F32 ? 4 : (fmt == FMT_F16Q8 && t == 2 ? 1 : 2);
+}
+// Bytes of one element summed over the planes.
+__host__ __device__ inline int format_bytes(int fmt) {
+    int b = 0;
+    for (int t = 0; t < format_terms(fmt); ++t) b += format_plane_bytes(fmt, t);
+    return b;
+}
 
 #if defined(__CUDACC__)
 // Read the value a split matrix stores at linear index idx (FP32 sum of terms).
 __device__ __forceinline__ float split_load(const SplitMat& m, int fmt, size_t idx) {
     if (fmt == FMT_F32) return static_cast<const float*>(m.term[0])[idx];
-    if (fmt == FMT_F16) {
+    if (fmt == FMT_F16 || fmt == FMT_F16Q8) {
         const __half* h = static_cast<const __half*>(m.term[0]);
         const __half* l = static_cast<const __half*>(m.term[1]);
         return (__half2float(h[idx]) + __half2float(l[idx])) * kF16Unscale;
@@ -64,7 +84,10 @@ __device__ __forceinline__ float split_load(const SplitMat& m, int fmt, size_t i
 // Split an FP32 value into its terms and store them at linear index idx.
 __device__ __forceinline__ void split_store(const SplitMat& m, int fmt, size_t idx, float v) {
     if (fmt == FMT_F32) { static_cast<float*>(m.term[0])[idx] = v; return; }
-    if (fmt == FMT_F16) {
+    if (fmt == FMT_F16 || fmt == FMT_F16Q8) {
+        if (fmt == FMT_F16Q8)
+            static_cast<__nv_fp8_storage_t*>(m.term[2])[idx] =
+                __nv_cvt_float_to_fp8(v * kE4M3Scale, __NV_SATFINITE, __NV_E4M3);
         v *= kF16Scale;
         __half h = __float2half_rn(v);
         __half l = __float2half_rn(v - __half2float(h));
@@ -90,7 +113,15 @@ __device__ __forceinline__ void split_store8(const SplitMat& m, int fmt, size_t 
         d[1] = make_float4(v[4], v[5], v[6], v[7]);
         return;
     }
-    if (fmt == FMT_F16) {
+    if (fmt == FMT_F16 || fmt == FMT_F16Q8) {
+        if (fmt == FMT_F16Q8) {
+            __align__(8) __nv_fp8x2_storage_t q[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                q[e] = __nv_cvt_float2_to_fp8x2(make_float2(v[2 * e] * kE4M3Scale, v[2 * e + 1] * kE4M3Scale),
+                                                __NV_SATFINITE, __NV_E4M3);
+            *reinterpret_cast<uint2*>(static_cast<uint8_t*>(m.term[2]) + idx) = *reinterpret_cast<const uint2*>(q);
+        }
         __align__(16) __half h[8];
         __align__(16) __half l[8];
 #pragma unroll
@@ -292,6 +323,17 @@ __device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t a_desc, uint6
         : "memory");
 }
 
+// The same with E4M3 operands: kind::f8f6f4, K = 32 elements (32 bytes) per MMA.
+__device__ __forceinline__ void umma_f8(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                        uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
 // Arrive on an mbarrier once every tcgen05 op issued so far by this thread completes.
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -437,6 +479,8 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
 // Instruction descriptor of tcgen05.mma kind::f16: FP32 accumulator
 // (bits 4-5 = 1), A/B format in bits 7-9 / 10-12 (0 = FP16, 1 = BF16),
 // both operands K-major (bits 15, 16 = 0), N >> 3 in bits 17-22, M >> 4 in bits 24-28.
+// (kind::f8f6f4 uses the same fields, format 0 = E4M3 for A and B, so
+// idesc_f16(M, N, false) also describes an E4M3 x E4M3 -> FP32 MMA.)
 __host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool bf16) {
     return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) |
            (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);

@@ -55,8 +55,8 @@ struct Step {
 // on steps 0-7; src/composite_FP16.cu:103-113: s = 1.01 on every step).
 std::vector<Step> schedule_steps(int schedule) {
     std::vector<Step> out;
-    if (schedule == PSDGB_SCHEDULE_FP16) {
-        const float s = 1.01f;
+    if (schedule == PSDGB_SCHEDULE_FP16 || schedule == PSDGB_SCHEDULE_FP8) {
+        const float s = schedule == PSDGB_SCHEDULE_FP8 ? 1.5f : 1.01f;
         for (auto& r : kCoeffFP16) {
             float a = static_cast<float>(r[0]), b = static_cast<float>(r[1]), c = static_cast<float>(r[2]);
             a /= s;
@@ -95,13 +95,17 @@ Layout make_layout(void* ws, int fmt, int64_t n) {
     Layout L{};
     L.fmt = fmt;
     L.np = pad128(n);
-    const size_t term = static_cast<size_t>(L.np) * L.np * format_elem_bytes(fmt);
+    const size_t elems = static_cast<size_t>(L.np) * L.np;
     const int nt = format_terms(fmt);
-    L.mat_bytes = term * nt;
+    L.mat_bytes = elems * format_bytes(fmt);
     char* base = static_cast<char*>(ws);
     SplitMat* mats[3] = {&L.A, &L.A2, &L.A3};
     for (int m = 0; m < 3; ++m) {
-        for (int t = 0; t < 3; ++t) mats[m]->term[t] = (t < nt) ? base + m * L.mat_bytes + t * term : nullptr;
+        size_t off = m * L.mat_bytes;
+        for (int t = 0; t < 3; ++t) {
+            mats[m]->term[t] = (t < nt) ? base + off : nullptr;
+            if (t < nt) off += elems * format_plane_bytes(fmt, t);
+        }
     }
     L.a32 = reinterpret_cast<float*>(L.A2.term[0]);
     L.ld = (n + 3) / 4 * 4;
@@ -216,12 +220,13 @@ bool precision_info(int precision, PrecisionInfo* out) {
         case PSDGB_PREC_BF16X3: *out = {FMT_BF16, 3, 2}; return true;
         case PSDGB_PREC_BF16X6: *out = {FMT_BF16, 6, 3}; return true;
         case PSDGB_PREC_BF16X9: *out = {FMT_BF16, 9, 3}; return true;
+        case PSDGB_PREC_FP8: *out = {FMT_F16Q8, 1, 1}; return true;
         default: return false;
     }
 }
 
 size_t split_matrix_bytes(int fmt, int64_t np) {
-    return static_cast<size_t>(np) * np * format_elem_bytes(fmt) * format_terms(fmt);
+    return static_cast<size_t>(np) * np * format_bytes(fmt);
 }
 
 psdgb_status gemm_symmetric(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
@@ -254,18 +259,14 @@ psdgb_status composite_enqueue(DeviceState* ds, int precision, int schedule, dou
         set_error("unknown precision");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) {
-        set_error("unknown schedule");
-        return PSDGB_ERR_INVALID_ARGUMENT;
-    }
-    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
-        // The FP32 table applies no safety factor on its last two steps; BF16
-        // operand rounding then pushes eigenvalues past 1 and the quintic diverges.
-        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+    if (const char* why = schedule_error(bulk_precision >= 0 ? bulk_precision : precision, schedule)) {
+        set_error(why);
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     if (n == 0) return PSDGB_OK;
-    const Layout L = make_layout(ws, pi.fmt, n);
+    // An FP8 bulk stores its operands in the F16Q8 format (the E4M3 plane for
+    // its products beside the FP16 pair the refinement reads).
+    const Layout L = make_layout(ws, bulk_precision == PSDGB_PREC_FP8 ? FMT_F16Q8 : pi.fmt, n);
     const double* up_dev = nullptr;
     const double* inv_up_dev = nullptr;
     if (auto_scale) {
@@ -319,8 +320,8 @@ psdgb_status composite_enqueue_f32(DeviceState* ds, int precision, int schedule,
         set_error("FP32 input needs a tensor-core precision");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
-    if (precision == PSDGB_PREC_BF16 && schedule != PSDGB_SCHEDULE_FP16) {
-        set_error("one-term BF16 products need the FP16 schedule (safety factor on every step)");
+    if (const char* why = schedule_error(precision, schedule)) {
+        set_error(why);
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
     if (n == 0) return PSDGB_OK;
@@ -361,7 +362,7 @@ psdgb_status composite_run(DeviceState* ds, int precision, int schedule, double*
 }  // namespace psdgb
 
 extern "C" int psdgb_filter_coefficients(int schedule, float* out, int cap) {
-    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16) return -1;
+    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16 && schedule != PSDGB_SCHEDULE_FP8) return -1;
     const std::vector<psdgb::Step> steps = psdgb::schedule_steps(schedule);
     for (int i = 0; i < cap && i < static_cast<int>(steps.size()); ++i) {
         out[3 * i] = steps[i].a;

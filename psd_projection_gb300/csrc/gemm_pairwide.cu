@@ -260,6 +260,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
                 if (q0 > p0 + 31) continue;  // above the diagonal: owned by the mirror
                 if (ep.fmt == FMT_F16)
                     epilogue_run<FMT_F16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
+                else if (ep.fmt == FMT_F16Q8)  // FP16 products after an FP8 bulk: keep the E4M3 plane too
+                    epilogue_run<FMT_F16Q8>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
                 else
                     epilogue_run<FMT_BF16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
             }

@@ -48,11 +48,15 @@ namespace {
 
 // ---- the kernel --------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false>
 __global__ void __launch_bounds__(64 + 32 * EW, 1)
     tc_group_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, const GroupWork gw, int num_tiles,
                     int* err) {
     using Cfg = TcCfg<TERMS>;
+    // E4M3 operands (FP8 = true): 128 elements per 128-byte K block,
+    // tcgen05.mma kind::f8f6f4 with K = 32 per instruction; the shared-memory
+    // geometry in bytes is that of the 16-bit operands.
+    constexpr int KBE = FP8 ? 2 * BK : BK;
     constexpr int STAGES = Cfg::STAGES;
     constexpr int STAGE_BYTES = Cfg::STAGE_BYTES;
     constexpr uint32_t IDESC = idesc_f16(BM, BN, BF16);
@@ -107,7 +111,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         bool stop = false;
         for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_half = tile_kblocks(ep, ti);
+            const int kb_half = tile_kblocks<KBE>(ep, ti);
             const int kb_total = kb_half * dual_mult;
             const int row_p = static_cast<int>(ti.blk.row_base + ti.bi * BM);
             const int row_q = static_cast<int>(ti.blk.row_base + ti.bj * BN);
@@ -130,7 +134,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 const bool second = kb >= kb_half;
                 const CUtensorMap* mp = second ? tm.Q : tm.P;
                 const CUtensorMap* mq = second ? tm.P : tm.Q;
-                const int kx = col0 + (second ? kb - kb_half : kb) * BK;
+                const int kx = col0 + (second ? kb - kb_half : kb) * KBE;
                 mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
 #pragma unroll
                 for (int t = 0; t < TERMS; ++t) tma_load_2d(st + t * TILE_BYTES, &mp[t], &full[s], kx, row_p);
@@ -146,7 +150,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         bool stop = false;
         for (int tile = blockIdx.x; tile < num_tiles && !stop; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_total = tile_kblocks(ep, ti) * dual_mult;
+            const int kb_total = tile_kblocks<KBE>(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
             if (!mbar_wait_bounded(&acc_empty[buf], use_ph ^ 1u)) {
@@ -176,7 +180,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                     for (int pi = 0; pi < NPROD; ++pi) {
                         const uint64_t ad = sdesc_kmajor_sw128(base + prod_a(pi) * TILE_BYTES + k * 32);
                         const uint64_t bd = sdesc_kmajor_sw128(base + (TERMS + prod_b(pi)) * TILE_BYTES + k * 32);
-                        umma_f16(acc, ad, bd, IDESC, (kb >= ACC_SPLIT || k != 0 || pi != 0) ? 1u : 0u);
+                        const uint32_t accum = (kb >= ACC_SPLIT || k != 0 || pi != 0) ? 1u : 0u;
+                        if (FP8)
+                            umma_f8(acc, ad, bd, IDESC, accum);
+                        else
+                            umma_f16(acc, ad, bd, IDESC, accum);
                     }
                 }
                 umma_commit(&empty[s]);
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         int it = 0;
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
-            const int kb_total = tile_kblocks(ep, ti) * dual_mult;
+            const int kb_total = tile_kblocks<KBE>(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
             if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {
@@ -207,9 +215,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
                 tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
             const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
             if (ep.fmt == FMT_F16)
-                epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
+                epilogue_tile<FMT_F16, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
+            else if (ep.fmt == FMT_F16Q8)
+                epilogue_tile<FMT_F16Q8, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
             else
-                epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
+                epilogue_tile<FMT_BF16, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -245,11 +255,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
 
 // ---- host side -------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false>
 psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
     using Cfg = TcCfg<TERMS>;
-    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW>;
+    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW, FP8>;
     static bool configured = false;  // attribute set once per process (per instantiation)
     if (!configured) {
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
@@ -257,6 +267,13 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
     }
     TmapSet tm;
     for (int t = 0; t < 3; ++t) {
+        if (FP8) {  // the E4M3 plane (term 2 of the F16Q8 format)
+            if (!make_tmap_u8(&tm.P[t], P.term[2], ld, rows, BM) || !make_tmap_u8(&tm.Q[t], Q.term[2], ld, rows, BM)) {
+                set_error("cuTensorMapEncodeTiled failed");
+                return PSDGB_ERR_CUDA;
+            }
+            continue;
+        }
         void* pb = (t < TERMS) ? P.term[t] : P.term[0];
         void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
         if (!make_tmap(&tm.P[t], pb, ld, rows, BF16, BM) || !make_tmap(&tm.Q[t], qb, ld, rows, BF16, BM)) {
@@ -274,19 +291,21 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
     return PSDGB_OK;
 }
 
-template <int TERMS, int NPROD, bool BF16>
+template <int TERMS, int NPROD, bool BF16, bool FP8 = false>
 psdgb_status launch_acc(DeviceState* ds, int acc_mode, const SplitMat& P, const SplitMat& Q, int64_t ld,
                         int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid,
                         cudaStream_t s) {
     switch (acc_mode) {
-        case ACC_4X1: return launch_tc<TERMS, NPROD, BF16, 4, 1, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
-        case ACC_2X2: return launch_tc<TERMS, NPROD, BF16, 2, 2, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_4X1:
+            return launch_tc<TERMS, NPROD, BF16, 4, 1, 4, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case ACC_2X2:
+            return launch_tc<TERMS, NPROD, BF16, 2, 2, 4, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         case ACC_1X4:
             // Short-K tiles (block-diagonal batches, small matrices) are
             // epilogue-bound: twice the epilogue warps, each on half the columns.
             if (g_group_epi_warps == 8)
-                return launch_tc<TERMS, NPROD, BF16, 1, 4, 8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
-            return launch_tc<TERMS, NPROD, BF16, 1, 4, 4>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+                return launch_tc<TERMS, NPROD, BF16, 1, 4, 8, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+            return launch_tc<TERMS, NPROD, BF16, 1, 4, 4, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         default: break;
     }
     set_error("gemm_tc: unknown accumulator mode");
@@ -323,6 +342,19 @@ bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16,
     return r == CUDA_SUCCESS;
 }
 
+bool make_tmap_u8(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, int box_rows) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(ld), static_cast<cuuint64_t>(rows)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(ld)};
+    const cuuint32_t box[2] = {128u, static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, base, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 bool make_tmap_f32(CUtensorMap* tm, const void* base, int64_t ld, int64_t rows, int64_t cols, int box_rows,
                    int box_cols) {
     auto fn = encode_fn();
@@ -342,6 +374,8 @@ psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const S
                            int grid, cudaStream_t s) {
     switch (precision) {
         case PSDGB_PREC_FP16: return launch_acc<1, 1, false>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+        case PSDGB_PREC_FP8:
+            return launch_acc<1, 1, false, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         case PSDGB_PREC_BF16: return launch_acc<1, 1, true>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         case PSDGB_PREC_FP16X3:
             return launch_acc<2, 3, false>(ds, acc_mode, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
@@ -363,10 +397,12 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
     const int64_t nt = np / BM;
     EpiParams e = ep;
     e.ld = static_cast<int>(np);
-    const bool three_terms = precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9;
+    // The E4M3 products run on 128 x 128 tiles only.
+    const bool three_terms =
+        precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9 || precision == PSDGB_PREC_FP8;
     int shape = g_tile_shape;
     if (shape < 0) shape = (!three_terms && np >= 2048) ? TILE_PAIR_256X256 : TILE_128X128;
-    if (nt >= 2 && shape == TILE_PAIR_256X128)
+    if (nt >= 2 && shape == TILE_PAIR_256X128 && precision != PSDGB_PREC_FP8)
         return gemm_tc_pair(ds, precision, auto_acc_mode(precision, np), P, Q, np, e, s);
     if (nt >= 2 && shape == TILE_WIDE_128X256 && !three_terms) return gemm_tc_wide(ds, precision, P, Q, np, e, s);
     if (nt >= 2 && shape == TILE_PAIR_256X256 && !three_terms)
@@ -387,7 +423,7 @@ int g_group_epi_warps = 8;
 // the accumulators instead so the epilogue overlaps the next tile (+4-10 %).
 int auto_acc_mode(int precision, int64_t np) {
     if (g_single_acc_mode >= 0) return g_single_acc_mode;
-    if (precision == PSDGB_PREC_FP16 || precision == PSDGB_PREC_BF16) return ACC_1X4;
+    if (precision == PSDGB_PREC_FP16 || precision == PSDGB_PREC_BF16 || precision == PSDGB_PREC_FP8) return ACC_1X4;
     if (np <= 2048) return ACC_1X4;
     if (np <= 4096) return ACC_2X2;
     return ACC_4X1;

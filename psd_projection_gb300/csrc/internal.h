@@ -80,6 +80,20 @@ struct PrecisionInfo {
 };
 bool precision_info(int precision, PrecisionInfo* out);
 inline int64_t pad128(int64_t n) { return (n + 127) / 128 * 128; }
+// Whether a precision may run a schedule (nullptr) or why not.  One-term BF16
+// operands round eigenvalues past 1 where the FP32 table's last two steps have
+// no safety factor, and the quintic diverges: BF16 needs a factor on every
+// step.  E4M3 operands (2^-4 rounding) diverge even with the FP16 table's
+// 1.01: FP8 runs the FP8 schedule.
+inline const char* schedule_error(int precision, int schedule) {
+    if (schedule != PSDGB_SCHEDULE_FP32 && schedule != PSDGB_SCHEDULE_FP16 && schedule != PSDGB_SCHEDULE_FP8)
+        return "unknown schedule";
+    if (precision == PSDGB_PREC_FP8 && schedule != PSDGB_SCHEDULE_FP8)
+        return "FP8 products need the FP8 schedule (safety factor 1.5 on every step)";
+    if (precision == PSDGB_PREC_BF16 && schedule == PSDGB_SCHEDULE_FP32)
+        return "one-term BF16 products need the FP16 schedule (safety factor on every step)";
+    return nullptr;
+}
 size_t split_matrix_bytes(int fmt, int64_t np);
 
 // ---- elementwise kernels (elem.cu) --------------------------------------------

@@ -17,6 +17,9 @@ namespace psdgb {
 // rows: 64 columns (128-byte rows) with the 128-byte swizzle, 32 columns
 // (64-byte rows) with the 64-byte swizzle (gemm_tc.cu).
 bool make_tmap(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, bool bf16, int box_rows, int box_cols = 64);
+// The same over a one-byte (E4M3) plane: boxes of 128 columns (128-byte rows,
+// 128-byte swizzle) x box_rows rows.
+bool make_tmap_u8(CUtensorMap* tm, void* base, int64_t ld, int64_t rows, int box_rows);
 
 namespace {
 
@@ -123,9 +126,11 @@ __device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiPara
 // padding is zero (ep.skip_pad), only the blocks that reach into the block's
 // n columns (the rest multiply zeros).  Producer, MMA issuer and epilogue
 // all use this count.
+// KBE: elements per K block (64 16-bit or 128 E4M3 elements: 128 bytes either way).
+template <int KBE = BK>
 __device__ __forceinline__ int tile_kblocks(const EpiParams& ep, const TileInfo& ti) {
-    if (!ep.skip_pad) return ti.blk.np / BK;
-    const int kb = (ti.blk.n + BK - 1) / BK;
+    if (!ep.skip_pad) return ti.blk.np / KBE;
+    const int kb = (ti.blk.n + KBE - 1) / KBE;
     return kb < 1 ? 1 : kb;
 }
 
@@ -137,10 +142,25 @@ __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag,
 // ---- epilogue helpers ------------------------------------------------------
 
 // Split 32 consecutive values and store them at element row_idx of every
-// term plane: 32 elements x 2 bytes per term = four 16-byte vectors.
+// term plane: 32 elements x 2 bytes per 16-bit term = four 16-byte vectors;
+// the E4M3 plane of the F16Q8 format takes two.
 template <int FMT>
 __device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, const float (&v)[32]) {
-    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+    constexpr int NT = FMT == FMT_BF16 ? 3 : 2;  // 16-bit planes
+    if (FMT == FMT_F16Q8) {
+        uint32_t q[8];
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+            const __nv_fp8x2_storage_t lo = __nv_cvt_float2_to_fp8x2(
+                make_float2(v[j] * kE4M3Scale, v[j + 1] * kE4M3Scale), __NV_SATFINITE, __NV_E4M3);
+            const __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(
+                make_float2(v[j + 2] * kE4M3Scale, v[j + 3] * kE4M3Scale), __NV_SATFINITE, __NV_E4M3);
+            q[j / 4] = static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
+        }
+        uint4* dst = reinterpret_cast<uint4*>(static_cast<uint8_t*>(m.term[2]) + row_idx);
+        dst[0] = make_uint4(q[0], q[1], q[2], q[3]);
+        dst[1] = make_uint4(q[4], q[5], q[6], q[7]);
+    }
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             uint32_t packed[16];
@@ -148,14 +168,14 @@ __device__ __forceinline__ void store_row32(const SplitMat& m, size_t row_idx, c
 #pragma unroll
             for (int j = 0; j < 32; j += 2) {
                 float x0 = v[j], x1 = v[j + 1];
-                if (FMT == FMT_F16) {
+                if (FMT != FMT_BF16) {
                     x0 *= kF16Scale;
                     x1 *= kF16Scale;
                 }
                 uint16_t h0 = 0, h1 = 0;
 #pragma unroll
                 for (int u = 0; u <= t; ++u) {
-                    if (FMT == FMT_F16) {
+                    if (FMT != FMT_BF16) {
                         __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
                         h0 = __half_as_ushort(a0);
                         h1 = __half_as_ushort(a1);
@@ -213,7 +233,7 @@ __device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, in
 // (FP16 terms: the sum times 2^-12).
 template <int FMT>
 __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (&out)[8]) {
-    constexpr int NT = FMT == FMT_F16 ? 2 : 3;
+    constexpr int NT = FMT == FMT_BF16 ? 3 : 2;  // the F16Q8 format's value is its F16 pair
 #pragma unroll
     for (int j = 0; j < 8; ++j) out[j] = 0.f;
 #pragma unroll
@@ -223,7 +243,7 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
             const uint16_t lo = static_cast<uint16_t>(ws[h] & 0xFFFFu), hi = static_cast<uint16_t>(ws[h] >> 16);
-            if (FMT == FMT_F16) {
+            if (FMT != FMT_BF16) {
                 out[2 * h] += __half2float(__ushort_as_half(lo));
                 out[2 * h + 1] += __half2float(__ushort_as_half(hi));
             } else {
@@ -232,7 +252,7 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
             }
         }
     }
-    if (FMT == FMT_F16) {
+    if (FMT != FMT_BF16) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) out[j] *= kF16Unscale;
     }
@@ -241,16 +261,20 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
 // The epilogue of one 32 x 32 run of accumulator values v (lane = row
 // p0 + lane, columns q0 .. q0 + 31, q0 <= p0 + 31): the final reconstruction
 // in FP64, or the polynomial step / plain store with the operand split, at
-// (p, q) and at the mirror (q, p).
-template <int FMT>
+// (p, q) and at the mirror (q, p).  FMT is the format the results are stored
+// in; E4M3_OPS says the product read the E4M3 plane (F16Q8 storage) rather
+// than the 16-bit terms.
+template <int FMT, bool E4M3_OPS = false>
 __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo& ti, int64_t p0, int64_t q0,
                                              float (&v)[32]) {
     const int64_t ld = ep.ld;
     const int64_t rb = ti.blk.row_base;
     const int64_t cb = ti.blk.col_base;
     const int64_t p = p0 + (threadIdx.x & 31);
-    // FP16-format operands carry a factor 2^12 each (kF16Scale).
-    const float acc_scale = FMT == FMT_F16 ? ep.acc_scale * kF16AccUnscale : ep.acc_scale;
+    // FP16 operand terms carry a factor 2^12 each (kF16Scale), E4M3 ones 2^7.
+    const float acc_scale = E4M3_OPS ? ep.acc_scale * kE4M3AccUnscale
+                            : FMT != FMT_BF16 ? ep.acc_scale * kF16AccUnscale
+                                              : ep.acc_scale;
     if (ep.kind == EPI_FINAL) {
         const int64_t n = ti.blk.n;
         if (p >= n) return;
@@ -308,7 +332,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
 // p0 + lane), reading the accumulators from TMEM, columns [c_begin, c_end)
 // of the tile.  TN is the tile width (the MMA's N): ti.bj counts column tiles
 // of TN, and the ACC_SPLIT accumulators of a tile sit TN TMEM columns apart.
-template <int FMT, int ACC_SPLIT, int TN = BN>
+template <int FMT, int ACC_SPLIT, int TN = BN, bool E4M3_OPS = false>
 __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc,
                               int c_begin = 0, int c_end = TN) {
     for (int c0 = c_begin; c0 < c_end; c0 += 32) {
@@ -325,7 +349,7 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
         }
         const int64_t q0 = ti.bj * TN + c0;
         if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
-        epilogue_run<FMT>(ep, ti, p0, q0, v);
+        epilogue_run<FMT, E4M3_OPS>(ep, ti, p0, q0, v);
     }
 }
 

@@ -4,8 +4,10 @@ compiled and run without MATLAB against a minimal stand-in of the MEX API
 on the GPU give, for every method string of the reference's wrapper
 (MATLAB/psd_projection_MATLAB.cu:93-166), the projection within the tolerance
 of the other GPU tests (1e-4 relative Frobenius against FP64 dsyevd for the
-FP32-class methods, 1e-3 for composite_FP16, 1e-10 for eig_FP64) and the
-eigenvalues as second output; an unknown method raises the reference's message.
+FP32-class methods, 1e-10 for eig_FP64, and for composite_FP16 1.05x the error
+of the oracle's restatement of the reference's FP16 method on the same input)
+and the eigenvalues as second output; an unknown method raises the
+reference's message.
 """
 import subprocess
 from pathlib import Path
@@ -37,7 +39,7 @@ def test_mex_source_compiles_and_links(tmp_path):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("method,tol", [("composite_FP32", 1e-4), ("composite_FP16", 1e-3),
+@pytest.mark.parametrize("method,tol", [("composite_FP32", 1e-4), ("composite_FP16", None),
                                         ("composite_FP32_emulated", 1e-4), ("eig_FP64", 1e-10),
                                         ("eig_FP32", 1e-4)])
 def test_mex_methods(tmp_path, method, tol):
@@ -55,6 +57,9 @@ def test_mex_methods(tmp_path, method, tol):
     assert r.returncode == 0, r.stdout + r.stderr
     out = np.fromfile(tmp_path / "out.bin").reshape(n, n).T
     proj, w = rp.eig_psd(x)
+    if tol is None:
+        ref, _ = rp.composite_auto_scale(x, "fp16")
+        tol = 1.05 * rp.rel_frobenius(ref, proj)
     assert rp.rel_frobenius(out, proj) <= tol
     if method.startswith("eig"):
         eigs = np.fromfile(tmp_path / "eigs.bin")
