@@ -247,7 +247,7 @@ def dense_equiv_flops(n: int, steps: int) -> float:
 
 def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 4096), n_streams: int = 64,
                   seed: int = 0, max_slots: int = 16, check_error: bool = False, admission: str = "fifo",
-                  priority_n: int = 0, reserve_sms: int = 0) -> dict:
+                  priority_n: int = 0, reserve_sms: int = 0, reserve_slots: int = 0) -> dict:
     """Closed-loop ADMM streams: stream k (n = sizes[k % 4]) waits an
     exponential think time (mean n_streams / offered_rate), perturbs its
     matrix by 1e-2 (E + E^T)/2, submits it, and waits for the projection
@@ -274,7 +274,7 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
     mean_think = n_streams / offered_rate
     lat, lat_by_n, gpu_ms = [], {n: [] for n in sizes}, []
     with Server(hbm_budget_bytes=64 << 30, max_slots=max_slots, warm_max_iter=10, admission=admission,
-                priority_n=priority_n, reserve_sms=reserve_sms) as srv:
+                priority_n=priority_n, reserve_sms=reserve_sms, reserve_slots=reserve_slots) as srv:
         # warm the per-(slot, n) graphs outside the measured window
         for k in range(min(n_streams, 2 * len(sizes))):
             srv.submit(k, mats[k], outs[k])
@@ -322,7 +322,8 @@ def serve_session(offered_rate: float, seconds: float, sizes=(64, 256, 1024, 409
             err = errs
     a = np.array(lat) * 1e3
     return {"offered_req_s": offered_rate, "admission": admission, "priority_n": priority_n,
-            "reserve_sms": reserve_sms, "throughput_req_s": completed / wall,
+            "reserve_sms": reserve_sms, "reserve_slots": reserve_slots, "max_slots": max_slots,
+            "throughput_req_s": completed / wall,
             "completed": completed,
             "p50_ms": float(np.percentile(a, 50)) if len(a) else None,
             "p99_ms": float(np.percentile(a, 99)) if len(a) else None,
@@ -661,9 +662,10 @@ def profile_case(kind: str, size: str) -> None:
 def serving_sessions(args) -> dict:
     sessions = [serve_session(r, args.serve_seconds, check_error=(r == 2000.0)) for r in (250.0, 500.0, 2000.0)]
     sessions += [serve_session(r, args.serve_seconds, admission="shortest_first") for r in (500.0, 2000.0)]
-    # Small requests (n <= 1024) on high-priority streams, 16 SMs kept free of the n = 4096 products.
-    sessions += [serve_session(2000.0, args.serve_seconds, admission=a, priority_n=1024, reserve_sms=16)
-                 for a in ("fifo", "shortest_first")]
+    # Small requests (n <= 1024) first: high-priority streams, 16 SMs kept free of the n = 4096 products,
+    # and 8 of 24 slots kept for them.
+    sessions += [serve_session(2000.0, args.serve_seconds, admission=a, max_slots=24, priority_n=1024,
+                               reserve_sms=16, reserve_slots=8) for a in ("fifo", "shortest_first")]
     return {"workload": "64 closed-loop ADMM-like streams, n uniform over {64,256,1024,4096} (16 streams each), "
                         "next matrix = previous + 1e-2 (E+E^T)/2, exponential think time for the offered rate; "
                         "fp16x3, warm-started Lanczos (10 steps), 16 slots, CUDA-graph replay",

@@ -251,6 +251,7 @@ typedef struct psdgb_server_config {
     int64_t priority_n;       /* > 0: requests with n <= priority_n run on high-priority streams and the
                                  persistent kernels of larger requests leave reserve_sms SMs free; 0: off */
     int reserve_sms;          /* SMs kept free of large requests' persistent kernels (with priority_n) */
+    int reserve_slots;        /* slots large requests may not take (with priority_n; < max_slots) */
 } psdgb_server_config;
 enum { PSDGB_ADMIT_FIFO = 0, PSDGB_ADMIT_SHORTEST_FIRST = 1 };
 

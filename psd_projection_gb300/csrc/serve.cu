@@ -22,12 +22,14 @@
 //   * CUDA graphs — with use_graphs, the whole projection of a given n on a
 //     slot is captured once and replayed (a few launches per request instead
 //     of ~100);
-//   * small requests first on the device — with priority_n > 0, requests of
-//     n <= priority_n run on high-priority streams, and the persistent
-//     kernels of larger requests are capped at (SMs - reserve_sms) CTAs, so
-//     reserve_sms SMs are always free of them: a small request's short kernels
-//     start at once instead of waiting for a large product kernel, which holds
-//     every SM it was given until it ends, to drain.
+//   * small requests first — with priority_n > 0, requests of n <= priority_n
+//     run on high-priority streams; the persistent kernels of larger requests
+//     are capped at (SMs - reserve_sms) CTAs, so reserve_sms SMs are always
+//     free of them (a small request's short kernels start at once instead of
+//     waiting for a large product kernel, which holds every SM it was given
+//     until it ends, to drain); and larger requests occupy at most
+//     (max_slots - reserve_slots) slots, so a small request never waits for
+//     a slot behind a wave of large ones.
 //
 // Every request's result depends only on its input and its key's previous
 // request: kernels are deterministic and a slot's buffers are private while
@@ -246,6 +248,12 @@ psdgb_status launch_request(psdgb_server* s, Slot& sl, const Request& r) {
 psdgb_status try_start(psdgb_server* s, const Request& r, bool* started, bool* no_slot) {
     *started = false;
     *no_slot = false;
+    if (s->cfg.priority_n > 0 && s->cfg.reserve_slots > 0 && !is_small(s->cfg, r.n)) {
+        int large = 0;
+        for (auto& sl : s->slots)
+            if (sl->busy && !is_small(s->cfg, sl->req.n)) ++large;
+        if (large >= s->cfg.max_slots - s->cfg.reserve_slots) return PSDGB_OK;  // not yet: slots kept for small ones
+    }
     Slot* pick = nullptr;
     for (auto& sl : s->slots)
         if (!sl->busy && sl->cap_n >= r.n && (!pick || sl->cap_n < pick->cap_n)) pick = sl.get();
@@ -330,7 +338,7 @@ double psdgb_clock_seconds(void) { return now_s(); }
 
 psdgb_status psdgb_server_create(const psdgb_server_config* cfg, psdgb_server** out) {
     if (!cfg || !out || cfg->max_slots <= 0 || cfg->max_slots > 256 || cfg->max_iter < 0 || cfg->warm_max_iter < 0 ||
-        cfg->priority_n < 0 || cfg->reserve_sms < 0 ||
+        cfg->priority_n < 0 || cfg->reserve_sms < 0 || cfg->reserve_slots < 0 || cfg->reserve_slots >= cfg->max_slots ||
         (cfg->admission != PSDGB_ADMIT_FIFO && cfg->admission != PSDGB_ADMIT_SHORTEST_FIRST)) {
         set_error("psdgb_server_create: bad configuration");
         return PSDGB_ERR_INVALID_ARGUMENT;

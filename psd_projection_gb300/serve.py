@@ -20,7 +20,7 @@ c_int, c_i64, c_u64, c_dbl, c_size = ctypes.c_int, ctypes.c_int64, ctypes.c_uint
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", c_size), ("max_slots", c_int), ("precision", c_int), ("schedule", c_int),
                 ("max_iter", c_i64), ("warm_max_iter", c_i64), ("use_graphs", c_int), ("admission", c_int),
-                ("priority_n", c_i64), ("reserve_sms", c_int)]
+                ("priority_n", c_i64), ("reserve_sms", c_int), ("reserve_slots", c_int)]
 
 
 class Completion(ctypes.Structure):
@@ -65,12 +65,14 @@ def clock() -> float:
 class Server:
     def __init__(self, hbm_budget_bytes: int = 16 << 30, max_slots: int = 8, precision: int = _capi.PREC_FP16X3,
                  schedule: int = _capi.SCHEDULE_FP32, max_iter: int = 20, warm_max_iter: int = 20,
-                 use_graphs: bool = True, admission: str = "fifo", priority_n: int = 0, reserve_sms: int = 0):
+                 use_graphs: bool = True, admission: str = "fifo", priority_n: int = 0, reserve_sms: int = 0,
+                 reserve_slots: int = 0):
         lib = _bind()
         if admission not in ("fifo", "shortest_first"):
             raise ValueError("admission is 'fifo' or 'shortest_first'")
         self.cfg = ServerConfig(hbm_budget_bytes, max_slots, precision, schedule, max_iter, warm_max_iter,
-                                1 if use_graphs else 0, 0 if admission == "fifo" else 1, priority_n, reserve_sms)
+                                1 if use_graphs else 0, 0 if admission == "fifo" else 1, priority_n, reserve_sms,
+                                reserve_slots)
         h = ctypes.c_void_p()
         _capi.check(lib.psdgb_server_create(ctypes.byref(self.cfg), ctypes.byref(h)), "psdgb_server_create")
         self._h = h

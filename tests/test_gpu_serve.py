@@ -33,7 +33,7 @@ def _streams(sizes, steps, seed=0):
 
 
 def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_iter=10, admission="fifo",
-           priority_n=0, reserve_sms=0):
+           priority_n=0, reserve_sms=0, reserve_slots=0):
     import torch
 
     from psd_projection_gb300.serve import Server
@@ -41,7 +41,7 @@ def _serve(seqs, max_slots, together, use_graphs=True, budget=8 << 30, warm_max_
     outs = {}
     with Server(hbm_budget_bytes=budget, max_slots=max_slots, use_graphs=use_graphs,
                 warm_max_iter=warm_max_iter, admission=admission, priority_n=priority_n,
-                reserve_sms=reserve_sms) as srv:
+                reserve_sms=reserve_sms, reserve_slots=reserve_slots) as srv:
         ins = {}
         order = []
         steps = len(seqs[0])
@@ -136,12 +136,14 @@ def test_shortest_first_admission_keeps_results_and_key_order():
 
 
 def test_priority_streams_and_sm_reserve_keep_results():
-    """Small requests on high-priority streams and large requests' persistent
-    kernels capped below the SM count: every result is still the one-at-a-time
-    result bit for bit (each tile and matvec partial is computed by one CTA in
-    a fixed order, whatever the grid)."""
-    seqs = _streams([64, 1024, 256, 2100, 64], steps=2, seed=5)
+    """Small requests on high-priority streams, large requests' persistent
+    kernels capped below the SM count and kept out of two of the six slots:
+    every result is still the one-at-a-time result bit for bit (each tile and
+    matvec partial is computed by one CTA in a fixed order, whatever the
+    grid), and everything is served."""
+    seqs = _streams([64, 1024, 256, 2100, 64, 1024, 2100], steps=2, seed=5)
     alone, _ = _serve(seqs, max_slots=1, together=False)
-    prio, _ = _serve(seqs, max_slots=6, together=True, priority_n=256, reserve_sms=24)
+    prio, _ = _serve(seqs, max_slots=6, together=True, priority_n=256, reserve_sms=24, reserve_slots=2)
+    assert set(prio) == set(alone)
     for kt in alone:
         assert np.array_equal(alone[kt], prio[kt]), kt
