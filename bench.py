@@ -622,6 +622,11 @@ def cpu_evd_projection_time(xs) -> float:
 # arms
 # ---------------------------------------------------------------------------
 
+def lib_check_error(psd) -> bool:
+    """True when a bounded device-side wait gave up during asynchronous work."""
+    return psd._capi.lib().psdgb_check_device_error() != 0
+
+
 def profile_case(kind: str, size: str) -> None:
     """Fixed small workloads to run under ncu (no timing, no oracle)."""
     import numpy as np
@@ -691,9 +696,15 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
 
     refill()
+    # The timed steps run through the asynchronous entry point: the host
+    # enqueues every step's projection ahead of the GPU (one workspace on one
+    # stream), so the GPU never waits for the host to launch the next step.
+    ws, lz = psd.async_buffers(n, prec)
     for i in range(W):
-        psd.composite(inputs[i], prec, sched, auto_scale=True)
+        psd.composite_async(inputs[i], ws, lz, prec, sched, stream=stream)
     torch.cuda.synchronize()
+    if lib_check_error(psd):
+        raise RuntimeError("device error in the warm-up steps")
 
     lib = psd._capi.lib()
     lib.psdgb_product_timing_read(None, None, None, 1)
@@ -705,10 +716,12 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         e0.record(stream)
         for i in range(K):
-            psd.composite(inputs[W + i], prec, sched, auto_scale=True)
+            psd.composite_async(inputs[W + i], ws, lz, prec, sched, stream=stream)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier(world)
+    if lib_check_error(psd):
+        raise RuntimeError("device error in the timed steps")
     lib.psdgb_product_timing_enable(0)
     launches = psd.kernel_launch_count() - launches0
     ms_total = e0.elapsed_time(e1)
@@ -731,7 +744,9 @@ def run_ours(args, rank, world):
     per_launch_flops = pfl.value / max(pl.value, 1)
     per_launch_ms = pms.value / max(pl.value, 1)
     achieved = per_launch_flops / (per_launch_ms / 1e3) / 1e12 if pl.value else None
-    peak = peaks["bf16_tflops_sustained"]
+    # Each product launch lasts about a millisecond and is timed alone by its
+    # own events: the burst peak is its denominator.
+    peak = peaks["bf16_tflops"]
     np_ = -(-n // 128) * 128
     wide = args.precision in ("fp16", "bf16", "fp16x3", "bf16x3") and np_ >= 2048
     kernel = (f"tc_pairwide_kernel (256x256 tiles on CTA pairs, tcgen05.mma.cta_group::2, {args.precision} split "
@@ -741,8 +756,9 @@ def run_ours(args, rank, world):
         "bound": "tensor", "kernel": kernel,
         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
         "frac": (achieved / peak) if achieved else None,
-        "peak_source": f"{peaks['source']} bf16_tflops_sustained (of {peaks['source']})",
-        "frac_of_burst": (achieved / peaks["bf16_tflops"]) if achieved and peaks.get("bf16_tflops") else None,
+        "peak_source": f"{peaks['source']} bf16_tflops (burst; of {peaks['source']})",
+        "frac_of_sustained": (achieved / peaks["bf16_tflops_sustained"])
+        if achieved and peaks.get("bf16_tflops_sustained") else None,
         "flops_per_launch": per_launch_flops, "ms_per_launch": per_launch_ms, "launches": pl.value,
         "flops_counted": "MMA flops of the lower-triangle 128x128 tiles: term products x 2 x 128 x 128 x K "
                          "per tile (K doubled for the final dual product); the 1.5 % of above-diagonal work the "

@@ -395,6 +395,31 @@ def composite_FP16_auto_scale_deflate(mat, k: int = 40, maxiter: int = 100, tol:
     _capi.check(st, "psdgb_composite_auto_scale_deflate_two_ends")
 
 
+def async_buffers(n: int, precision: int = PREC_FP16X3, max_iter: int = 20):
+    """Device buffers for composite_async: (workspace, Lanczos state), uint8 CUDA tensors."""
+    torch = _torch()
+    ws = torch.empty(max(workspace_size(n, precision), 1), dtype=torch.uint8, device="cuda")
+    lz = torch.empty(max(_capi.lib().psdgb_lanczos_state_size(n, max_iter), 1), dtype=torch.uint8, device="cuda")
+    return ws, lz
+
+
+def composite_async(mat, workspace, lanczos_state, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32,
+                    max_iter: int = 20, tol: float = 1e-10, seed: int = DEFAULT_SEED,
+                    residual: int = RESIDUAL_REFERENCE, warm_start=None, ritz_out=None, stream=None) -> None:
+    """The auto-scaled projection of mat, in place, enqueued on the stream with
+    no host synchronisation and no allocation (psdgb_composite_auto_scale_async);
+    workspace / lanczos_state from async_buffers.  Calls on one stream may
+    share the buffers; calls in flight on different streams may not."""
+    n = _check_mat(mat)
+    st = _capi.lib().psdgb_composite_auto_scale_async(
+        int(precision), int(schedule), ctypes.c_void_p(mat.data_ptr()), n, int(max_iter), float(tol), int(seed),
+        int(residual), ctypes.c_void_p(warm_start.data_ptr()) if warm_start is not None else None,
+        ctypes.c_void_p(ritz_out.data_ptr()) if ritz_out is not None else None,
+        ctypes.c_void_p(workspace.data_ptr()), workspace.numel(), ctypes.c_void_p(lanczos_state.data_ptr()),
+        lanczos_state.numel(), _stream_ptr(stream))
+    _capi.check(st, "psdgb_composite_auto_scale_async")
+
+
 def composite_f32(mat, precision: int = PREC_FP16X3, schedule: int = SCHEDULE_FP32, max_iter: int = 20,
                   tol: float = 1e-10, seed: int = DEFAULT_SEED, residual: int = RESIDUAL_REFERENCE, warm_start=None,
                   ritz_out=None, stream=None) -> None:

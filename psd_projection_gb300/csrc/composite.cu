@@ -112,9 +112,13 @@ Layout make_layout(void* ws, int fmt, int64_t n) {
     return L;
 }
 
-EpiParams epi_base(const Layout& L, int64_t n) {
+// Epilogue parameters of a product at `precision` on layout L.  Only E4M3
+// products read the F16Q8 format's E4M3 plane; the FP16 products that refine
+// an FP8 bulk read and write the FP16 pair alone (planes 0 and 1, laid out as
+// the F16 format), so their epilogues store the F16 format.
+EpiParams epi_base(const Layout& L, int64_t n, int precision) {
     EpiParams ep{};
-    ep.fmt = L.fmt;
+    ep.fmt = (L.fmt == FMT_F16Q8 && precision != PSDGB_PREC_FP8) ? FMT_F16 : L.fmt;
     ep.np = static_cast<int>(L.np);
     ep.n = static_cast<int>(n);
     ep.acc_scale = 1.0f;
@@ -135,11 +139,11 @@ psdgb_status run_step(DeviceState* ds, int precision, const Step& st, const Layo
     // third product dual alone, 1.02-1.03x with both.)
     const bool dual_step = pi.nprod == 1;
     {
-        EpiParams e1 = epi_base(L, n);
+        EpiParams e1 = epi_base(L, n, precision);
         e1.kind = EPI_STORE;
         e1.out = L.A2;
         PSDGB_TRY(gemm_symmetric(ds, precision, L.A, L.A, L.np, e1, s));  // A2 = A * A
-        EpiParams e2 = epi_base(L, n);
+        EpiParams e2 = epi_base(L, n, precision);
         e2.kind = EPI_STORE;
         e2.out = L.A3;
         if (dual_step) {
@@ -147,7 +151,7 @@ psdgb_status run_step(DeviceState* ds, int precision, const Step& st, const Layo
             e2.acc_scale = 0.5f;
         }
         PSDGB_TRY(gemm_symmetric(ds, precision, L.A2, L.A, L.np, e2, s));  // A3 = A2 * A
-        EpiParams e3 = epi_base(L, n);
+        EpiParams e3 = epi_base(L, n, precision);
         e3.kind = EPI_STEP;
         e3.a = st.a;
         e3.b = st.b;
@@ -184,7 +188,7 @@ psdgb_status run_filter(DeviceState* ds, int precision, int schedule, const Layo
 psdgb_status run_final(DeviceState* ds, int precision, const Layout& L, double* mat, int64_t n, const double* up_dev,
                        const double* inv_up_dev, cudaStream_t s, double up_host = 1.0) {
     PSDGB_CUDA_TRY(launch_split_from_f64_upper(mat, n, 1.0 / up_host, inv_up_dev, L.A2, L.fmt, L.np, s));
-    EpiParams ef = epi_base(L, n);
+    EpiParams ef = epi_base(L, n, precision);
     ef.kind = EPI_FINAL;
     ef.up = up_host;
     ef.up_dev = up_dev;
@@ -334,7 +338,7 @@ psdgb_status composite_enqueue_f32(DeviceState* ds, int precision, int schedule,
     PSDGB_CUDA_TRY(launch_split_from_f32(L.a32, n, L.ld, 1.0, inv_up_dev, L.A, L.fmt, L.np, s));
     PSDGB_TRY(run_filter(ds, precision, schedule, L, n, s, -1, 0));
     PSDGB_CUDA_TRY(launch_split_from_f32_upper(mat, n, 1.0, inv_up_dev, L.A2, L.fmt, L.np, s));
-    EpiParams ef = epi_base(L, n);
+    EpiParams ef = epi_base(L, n, precision);
     ef.kind = EPI_FINAL32;
     ef.up = 1.0;
     ef.up_dev = up_dev;

@@ -43,8 +43,8 @@ struct PairWideCfg {
 };
 
 struct TmapPW {
-    CUtensorMap Pa[2];  // P, boxes of 128 rows (A operand; B of a dual product's second half)
-    CUtensorMap Qa[2];  // Q, 128 rows
+    CUtensorMap Pa[3];  // P's term planes, boxes of 128 rows (A operand; B of a dual product's second half)
+    CUtensorMap Qa[3];  // Q's term planes, 128 rows
 };
 
 template <int KB>
@@ -56,7 +56,10 @@ __device__ __forceinline__ uint64_t sdesc_pw(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
+// One CTA per SM: the whole register file for its PW_THREADS threads
+// (200 x 320 = 64000 of 65536); the default cap of 168 spilled 2 KB of the
+// epilogue's K-chunk sums per thread.
+__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(200)
     tc_pairwide_kernel(const __grid_constant__ TmapPW tm, const EpiParams ep, int group_rows, int num_pairs,
                        int* err) {
     using Cfg = PairWideCfg<TERMS, KB>;
@@ -260,8 +263,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
                 if (q0 > p0 + 31) continue;  // above the diagonal: owned by the mirror
                 if (ep.fmt == FMT_F16)
                     epilogue_run<FMT_F16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
-                else if (ep.fmt == FMT_F16Q8)  // FP16 products after an FP8 bulk: keep the E4M3 plane too
-                    epilogue_run<FMT_F16Q8>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
                 else
                     epilogue_run<FMT_BF16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
             }
@@ -323,7 +324,7 @@ psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat&
         max_clusters = n;
     }
     TmapPW tm;
-    for (int t = 0; t < 2; ++t) {
+    for (int t = 0; t < 3; ++t) {
         void* pb = (t < TERMS) ? P.term[t] : P.term[0];
         void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
         if (!make_tmap(&tm.Pa[t], pb, np, np, BF16, BM, KB) || !make_tmap(&tm.Qa[t], qb, np, np, BF16, BM, KB)) {
@@ -345,7 +346,9 @@ psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat&
 
 }  // namespace
 
-// One- and two-term precisions (the three-term ones keep the single-CTA kernel).
+// One-, two- and three-term precisions.  Three BF16 terms take K blocks of 32
+// (64-byte swizzle): 48 KB stages, four of them in shared memory; chunks of
+// 32 K blocks (K = 1024) per TMEM slot, as for the others.
 psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                               const EpiParams& ep, cudaStream_t s) {
     constexpr int WHOLE = 1 << 20;
@@ -361,6 +364,8 @@ psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P,
         case PSDGB_PREC_BF16: return launch_pairwide<1, 1, true, WHOLE, 64>(ds, P, Q, np, ep, s);
         case PSDGB_PREC_FP16X3: return launch_pairwide<2, 3, false, 16, 64>(ds, P, Q, np, ep, s);
         case PSDGB_PREC_BF16X3: return launch_pairwide<2, 3, true, 16, 64>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16X6: return launch_pairwide<3, 6, true, 32, 32>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_BF16X9: return launch_pairwide<3, 9, true, 32, 32>(ds, P, Q, np, ep, s);
         default: break;
     }
     set_error("gemm_tc_pairwide: precision not served by 256 x 256 pair tiles");

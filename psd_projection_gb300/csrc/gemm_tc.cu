@@ -397,16 +397,18 @@ psdgb_status gemm_tc(DeviceState* ds, int precision, const SplitMat& P, const Sp
     const int64_t nt = np / BM;
     EpiParams e = ep;
     e.ld = static_cast<int>(np);
-    // The E4M3 products run on 128 x 128 tiles only.
-    const bool three_terms =
-        precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9 || precision == PSDGB_PREC_FP8;
+    // The E4M3 products run on 128 x 128 tiles only; three-term products also
+    // run on 256 x 256 pair tiles, not on 128 x 256 single-CTA tiles (whose
+    // stages would not fit twice in shared memory).
+    const bool fp8 = precision == PSDGB_PREC_FP8;
+    const bool three_terms = precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9;
     int shape = g_tile_shape;
-    if (shape < 0) shape = (!three_terms && np >= 2048) ? TILE_PAIR_256X256 : TILE_128X128;
-    if (nt >= 2 && shape == TILE_PAIR_256X128 && precision != PSDGB_PREC_FP8)
+    if (shape < 0) shape = (!fp8 && np >= 2048) ? TILE_PAIR_256X256 : TILE_128X128;
+    if (nt >= 2 && shape == TILE_PAIR_256X128 && !fp8)
         return gemm_tc_pair(ds, precision, auto_acc_mode(precision, np), P, Q, np, e, s);
-    if (nt >= 2 && shape == TILE_WIDE_128X256 && !three_terms) return gemm_tc_wide(ds, precision, P, Q, np, e, s);
-    if (nt >= 2 && shape == TILE_PAIR_256X256 && !three_terms)
-        return gemm_tc_pairwide(ds, precision, P, Q, np, e, s);
+    if (nt >= 2 && shape == TILE_WIDE_128X256 && !three_terms && !fp8)
+        return gemm_tc_wide(ds, precision, P, Q, np, e, s);
+    if (nt >= 2 && shape == TILE_PAIR_256X256 && !fp8) return gemm_tc_pairwide(ds, precision, P, Q, np, e, s);
     GroupWork gw{nullptr, nullptr, g_tile_group_rows};
     return gemm_tc_group(ds, precision, auto_acc_mode(precision, np), P, Q, np, np, e, gw, nt * (nt + 1) / 2, 0, s);
 }

@@ -262,8 +262,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
                 const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
                 if (ep.fmt == FMT_F16)
                     epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
-                else if (ep.fmt == FMT_F16Q8)
-                    epilogue_tile<FMT_F16Q8, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
                 else
                     epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
             }

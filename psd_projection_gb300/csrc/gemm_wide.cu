@@ -120,7 +120,8 @@ __device__ __forceinline__ uint64_t sdesc_kb(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-__global__ void __launch_bounds__(W_THREADS, 1)
+// One CTA per SM: the whole register file for its W_THREADS threads (see gemm_pairwide.cu).
+__global__ void __maxnreg__(200)
     tc_wide_kernel(const __grid_constant__ TmapWideSet tm, const EpiParams ep, int group_rows, int num_tiles,
                    int* err) {
     using Cfg = WideCfg<TERMS, KB>;
@@ -314,8 +315,6 @@ __global__ void __launch_bounds__(W_THREADS, 1)
                 if (q0 > p0 + 31) continue;  // above the diagonal: owned by the mirror
                 if (ep.fmt == FMT_F16)
                     epilogue_run<FMT_F16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
-                else if (ep.fmt == FMT_F16Q8)  // FP16 products after an FP8 bulk: keep the E4M3 plane too
-                    epilogue_run<FMT_F16Q8>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
                 else
                     epilogue_run<FMT_BF16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
             }

@@ -141,93 +141,75 @@ __device__ __forceinline__ void record_error(int* err, volatile int* abort_flag,
 
 // ---- epilogue helpers ------------------------------------------------------
 
-// The terms of 32 consecutive values, computed once for a row and its
-// mirror: 16-bit plane t, word j / 2 holds elements j (low half) and j + 1;
-// for the F16Q8 format q8 word j / 4 holds the E4M3 bytes of elements j to
-// j + 3 (lowest byte first).  The arithmetic is split_store's, so both give
-// the same bits.
+// Store a 32 x 32 run of the warp (lane = local row p0 + lane, columns
+// q0..q0+31, every element strictly below the diagonal) and its mirror, one
+// term plane at a time: the plane's 32 terms are computed once (the
+// arithmetic of split_store, so both give the same bits) and written to the
+// row as 16-byte vectors (four per 16-bit plane, two for the E4M3 plane) and
+// to the mirror (rows q0..q0+31, column p0 + lane) element by element, which
+// the warp's 32 lanes coalesce into contiguous 64-byte stores.  One plane's
+// terms at a time keeps 16 words live.  (Transposing the mirror through
+// shared memory to write it as vectors measured 2-3 % slower.)
 template <int FMT>
-struct Run32Terms {
-    static constexpr int NT = FMT == FMT_BF16 ? 3 : 2;  // 16-bit planes
-    uint32_t pk[NT][16];
-    uint32_t q8[FMT == FMT_F16Q8 ? 8 : 1];
-};
-
-template <int FMT>
-__device__ __forceinline__ void split_run32(const float (&v)[32], Run32Terms<FMT>& r) {
-    constexpr int NT = Run32Terms<FMT>::NT;
+__device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p0,
+                                               int64_t q0, const float (&v)[32]) {
+    constexpr int NT = FMT == FMT_BF16 ? 3 : 2;  // 16-bit planes
+    const int64_t p = p0 + (threadIdx.x & 31);
+    const size_t row_idx = static_cast<size_t>(rb + p) * ld + cb + q0;
+    const size_t mir_idx = static_cast<size_t>(rb + q0) * ld + cb + p;
     if (FMT == FMT_F16Q8) {
+        uint32_t q[8];  // word j / 4: the E4M3 bytes of elements j .. j + 3, lowest first
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
             const __nv_fp8x2_storage_t lo = __nv_cvt_float2_to_fp8x2(
                 make_float2(v[j] * kE4M3Scale, v[j + 1] * kE4M3Scale), __NV_SATFINITE, __NV_E4M3);
             const __nv_fp8x2_storage_t hi = __nv_cvt_float2_to_fp8x2(
                 make_float2(v[j + 2] * kE4M3Scale, v[j + 3] * kE4M3Scale), __NV_SATFINITE, __NV_E4M3);
-            r.q8[j / 4] = static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
+            q[j / 4] = static_cast<uint32_t>(lo) | (static_cast<uint32_t>(hi) << 16);
         }
-    }
+        uint8_t* plane = static_cast<uint8_t*>(m.term[2]);
+        uint4* dst = reinterpret_cast<uint4*>(plane + row_idx);
+        dst[0] = make_uint4(q[0], q[1], q[2], q[3]);
+        dst[1] = make_uint4(q[4], q[5], q[6], q[7]);
 #pragma unroll
-    for (int j = 0; j < 32; j += 2) {
-        float x0 = v[j], x1 = v[j + 1];
-        if (FMT != FMT_BF16) {
-            x0 *= kF16Scale;
-            x1 *= kF16Scale;
-        }
-#pragma unroll
-        for (int t = 0; t < NT; ++t) {
-            uint16_t h0, h1;
-            if (FMT != FMT_BF16) {
-                const __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
-                h0 = __half_as_ushort(a0);
-                h1 = __half_as_ushort(a1);
-                x0 -= __half2float(a0);
-                x1 -= __half2float(a1);
-            } else {
-                const __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
-                h0 = __bfloat16_as_ushort(a0);
-                h1 = __bfloat16_as_ushort(a1);
-                x0 -= __bfloat162float(a0);
-                x1 -= __bfloat162float(a1);
-            }
-            r.pk[t][j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
-        }
+        for (int j = 0; j < 32; ++j) plane[mir_idx + static_cast<size_t>(j) * ld] = static_cast<uint8_t>(q[j >> 2] >> ((j & 3) * 8));
     }
-}
-
-// Store a 32 x 32 run of the warp (lane = local row p0 + lane, columns
-// q0..q0+31, every element strictly below the diagonal) and its mirror, the
-// terms split once.  The row is written as 16-byte vectors (four per 16-bit
-// plane, two for the E4M3 plane); the mirror (rows q0..q0+31, column
-// p0 + lane) element by element, which the warp's 32 lanes coalesce into
-// contiguous 64-byte stores.  (Transposing the mirror through shared memory
-// to write it as vectors measured 2-3 % slower.)
-template <int FMT>
-__device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p0,
-                                               int64_t q0, const float (&v)[32]) {
-    constexpr int NT = Run32Terms<FMT>::NT;
-    const int64_t p = p0 + (threadIdx.x & 31);
-    Run32Terms<FMT> r;
-    split_run32<FMT>(v, r);
-    const size_t row_idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
-        uint4* dst = reinterpret_cast<uint4*>(static_cast<uint16_t*>(m.term[t]) + row_idx);
+        uint32_t pk[16];  // word j / 2: the terms of elements j (low half) and j + 1
 #pragma unroll
-        for (int u = 0; u < 4; ++u) dst[u] = make_uint4(r.pk[t][4 * u], r.pk[t][4 * u + 1], r.pk[t][4 * u + 2], r.pk[t][4 * u + 3]);
-    }
-    if (FMT == FMT_F16Q8) {
-        uint4* dst = reinterpret_cast<uint4*>(static_cast<uint8_t*>(m.term[2]) + row_idx);
-        dst[0] = make_uint4(r.q8[0], r.q8[1], r.q8[2], r.q8[3]);
-        dst[1] = make_uint4(r.q8[4], r.q8[5], r.q8[6], r.q8[7]);
-    }
+        for (int j = 0; j < 32; j += 2) {
+            float x0 = v[j], x1 = v[j + 1];
+            if (FMT != FMT_BF16) {
+                x0 *= kF16Scale;
+                x1 *= kF16Scale;
+            }
+            uint16_t h0 = 0, h1 = 0;
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-        const size_t mi = static_cast<size_t>(rb + q0 + j) * ld + cb + p;
+            for (int u = 0; u <= t; ++u) {
+                if (FMT != FMT_BF16) {
+                    const __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
+                    h0 = __half_as_ushort(a0);
+                    h1 = __half_as_ushort(a1);
+                    x0 -= __half2float(a0);
+                    x1 -= __half2float(a1);
+                } else {
+                    const __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
+                    h0 = __bfloat16_as_ushort(a0);
+                    h1 = __bfloat16_as_ushort(a1);
+                    x0 -= __bfloat162float(a0);
+                    x1 -= __bfloat162float(a1);
+                }
+            }
+            pk[j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
+        }
+        uint16_t* plane = static_cast<uint16_t*>(m.term[t]);
+        uint4* dst = reinterpret_cast<uint4*>(plane + row_idx);
 #pragma unroll
-        for (int t = 0; t < NT; ++t)
-            static_cast<uint16_t*>(m.term[t])[mi] = static_cast<uint16_t>(r.pk[t][j >> 1] >> ((j & 1) * 16));
-        if (FMT == FMT_F16Q8)
-            static_cast<uint8_t*>(m.term[2])[mi] = static_cast<uint8_t>(r.q8[(j >> 2) & 7] >> ((j & 3) * 8));
+        for (int u = 0; u < 4; ++u) dst[u] = make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            plane[mir_idx + static_cast<size_t>(j) * ld] = static_cast<uint16_t>(pk[j >> 1] >> ((j & 1) * 16));
     }
 }
 

@@ -420,3 +420,25 @@ def test_pair_wide_tiles_match_wide(psd, precision, n):
         psd.set_product_tuning(psd.TUNE_TILE_SHAPE, prev)
     assert np.linalg.norm(pair - wide) <= 1e-6 * np.linalg.norm(wide)
     assert rp.rel_frobenius(pair, proj) <= (2e-3 if precision == "fp16" else 1e-4)
+
+
+@pytest.mark.parametrize("precision", ["bf16x9", "bf16x6"])
+@pytest.mark.parametrize("n", [300, 2100])
+def test_three_term_pair_tiles_match_single_cta_tiles(psd, precision, n):
+    """Three-term BF16 products on 256 x 256 pair tiles (32-wide K blocks, K
+    summed in register chunks of 1024 — the default from n = 2048) against
+    the 128 x 128 single-CTA kernel: both within the FP32-class bar of the FP64
+    EVD projection, and within 1e-5 of each other (the K summation order
+    differs)."""
+    x = uniform_spectrum(n, 2.0, seed=80 + n)
+    proj, _ = rp.eig_psd(x)
+    prev_shape = psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_128X128)
+    try:
+        single, _ = run(psd, x, precision, auto_scale=True)
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, psd.TILE_PAIR_256X256)
+        pair, _ = run(psd, x, precision, auto_scale=True)
+    finally:
+        psd.set_product_tuning(psd.TUNE_TILE_SHAPE, prev_shape)
+    assert rp.rel_frobenius(single, proj) <= 1e-4
+    assert rp.rel_frobenius(pair, proj) <= 1e-4
+    assert np.linalg.norm(pair - single) <= 1e-5 * np.linalg.norm(single)
