@@ -56,10 +56,10 @@ __device__ __forceinline__ uint64_t sdesc_pw(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-// One CTA per SM: the whole register file for its PW_THREADS threads
-// (200 x 320 = 64000 of 65536); the default cap of 168 spilled 2 KB of the
-// epilogue's K-chunk sums per thread.
-__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(200)
+// One CTA per SM: 192 registers for each of its PW_THREADS threads (61440 of
+// the SM's 65536; 200 each was refused at launch).  Under the default cap of
+// 168 the epilogue's 128 K-chunk sums per thread spilled 2.1 KB, 0.6 KB at 192.
+__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(192)
     tc_pairwide_kernel(const __grid_constant__ TmapPW tm, const EpiParams ep, int group_rows, int num_pairs,
                        int* err) {
     using Cfg = PairWideCfg<TERMS, KB>;

@@ -120,8 +120,8 @@ __device__ __forceinline__ uint64_t sdesc_kb(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-// One CTA per SM: the whole register file for its W_THREADS threads (see gemm_pairwide.cu).
-__global__ void __maxnreg__(200)
+// One CTA per SM: 192 registers for each of its W_THREADS threads (see gemm_pairwide.cu).
+__global__ void __maxnreg__(192)
     tc_wide_kernel(const __grid_constant__ TmapWideSet tm, const EpiParams ep, int group_rows, int num_tiles,
                    int* err) {
     using Cfg = WideCfg<TERMS, KB>;
