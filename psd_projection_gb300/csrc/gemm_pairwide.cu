@@ -56,10 +56,7 @@ __device__ __forceinline__ uint64_t sdesc_pw(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-// One CTA per SM: 192 registers for each of its PW_THREADS threads (61440 of
-// the SM's 65536; 200 each was refused at launch).  Under the default cap of
-// 168 the epilogue's 128 K-chunk sums per thread spilled 2.1 KB, 0.6 KB at 192.
-__global__ void __cluster_dims__(2, 1, 1) __maxnreg__(192)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
     tc_pairwide_kernel(const __grid_constant__ TmapPW tm, const EpiParams ep, int group_rows, int num_pairs,
                        int* err) {
     using Cfg = PairWideCfg<TERMS, KB>;
@@ -261,10 +258,10 @@ __global__ void __cluster_dims__(2, 1, 1) __maxnreg__(192)
             for (int r = 0; r < 4; ++r) {
                 const int64_t q0 = qbase + 32 * r;
                 if (q0 > p0 + 31) continue;  // above the diagonal: owned by the mirror
-                if (ep.fmt == FMT_F16)
-                    epilogue_run<FMT_F16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
-                else
-                    epilogue_run<FMT_BF16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
+                // The storage format follows the operand type (ep.fmt is FP16 for
+                // FP16 operands, BF16 for BF16 ones): one epilogue per instantiation.
+                epilogue_run<BF16 ? FMT_BF16 : FMT_F16>(ep, ti, p0, q0,
+                                                        *reinterpret_cast<float(*)[32]>(sum + 32 * r));
             }
         }
     }

@@ -120,8 +120,7 @@ __device__ __forceinline__ uint64_t sdesc_kb(uint32_t saddr) {
 }
 
 template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-// One CTA per SM: 192 registers for each of its W_THREADS threads (see gemm_pairwide.cu).
-__global__ void __maxnreg__(192)
+__global__ void __launch_bounds__(W_THREADS, 1)
     tc_wide_kernel(const __grid_constant__ TmapWideSet tm, const EpiParams ep, int group_rows, int num_tiles,
                    int* err) {
     using Cfg = WideCfg<TERMS, KB>;
@@ -313,10 +312,10 @@ __global__ void __maxnreg__(192)
             for (int r = 0; r < 4; ++r) {
                 const int64_t q0 = qbase + 32 * r;
                 if (q0 > p0 + 31) continue;  // above the diagonal: owned by the mirror
-                if (ep.fmt == FMT_F16)
-                    epilogue_run<FMT_F16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
-                else
-                    epilogue_run<FMT_BF16>(ep, ti, p0, q0, *reinterpret_cast<float(*)[32]>(sum + 32 * r));
+                // The storage format follows the operand type (ep.fmt is FP16 for
+                // FP16 operands, BF16 for BF16 ones): one epilogue per instantiation.
+                epilogue_run<BF16 ? FMT_BF16 : FMT_F16>(ep, ti, p0, q0,
+                                                        *reinterpret_cast<float(*)[32]>(sum + 32 * r));
             }
         }
     }
