@@ -199,11 +199,21 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         constexpr int SLICE = BN / (EW / 4);
         const int c_begin = ((warp - 2) / 4) * SLICE;
         int it = 0;
+        // The step epilogue's inputs are requested one tile ahead (the MMAs run
+        // up to ACC_BUFS tiles ahead, so the epilogue rarely waits for them).
+        if (blockIdx.x < num_tiles) {
+            const TileInfo t0 = tile_info(gw, ep, blockIdx.x);
+            prefetch_step_inputs(ep, t0, t0.bi * BM + q4 * 32, BN, c_begin, c_begin + SLICE);
+        }
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
             const int kb_total = tile_kblocks<KBE>(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
+            if (tile + static_cast<int>(gridDim.x) < num_tiles) {
+                const TileInfo tn = tile_info(gw, ep, tile + gridDim.x);
+                prefetch_step_inputs(ep, tn, tn.bi * BM + q4 * 32, BN, c_begin, c_begin + SLICE);
+            }
             if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {
                 record_error(err, abort_flag, DEVERR_EPI_WAIT);
                 break;
