@@ -47,7 +47,7 @@ METRIC = "n=8192 proj/s & TC TFLOP/s vs plain FP32 at equal error; p50/p99 serve
 
 # DRAM bytes (read + write) of one product launch, from one ncu capture of the
 # same kernel on the same workload size (profiles/ holds the summary).
-TRAFFIC_PER_LAUNCH = {(8192, "fp16x3", True): 1.67e9}
+TRAFFIC_PER_LAUNCH = {(8192, "fp16x3", True): 1.72e9}
 TRAFFIC_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch (profiles/tc_pairwide_kernel_fp16x3_n8192.md)"
 
 
