@@ -166,100 +166,12 @@ __device__ void cta_matvec_cols(const float* __restrict__ A, int n, int ld4, con
     }
 }
 
-// Blocks up to this size read only the lower 32 x 32 tiles of their FP32 copy
-// in the Lanczos matvecs (cta_matvec_tri).
-constexpr int TRI_MAX_N = 512;
-// Shared memory for cta_matvec_tri's per-tile partial sums (row and column
-// sums, 32 floats each, per lower tile), zero above TRI_MAX_N.
-__host__ __device__ inline int tri_part_floats(int n) {
-    if (n <= 128 || n > TRI_MAX_N) return 0;
-    const int nt = (n + 31) / 32;
-    return nt * (nt + 1) / 2 * 64;
-}
-
-// y = A x for a symmetric block from the lower 32 x 32 tiles of its FP32
-// copy only (half the bytes of cta_matvec).  Warps take the lower tiles
-// (bi, bj), bj <= bi, round-robin; lane c holds column bj*32 + c of the
-// tile.  An off-diagonal tile gives the row sums of its tile row (A_ij x_j,
-// a recursive-halving shuffle reduction) and the column sums of its tile
-// column (A_ij^T x_i, one column per lane); a diagonal tile (stored in full)
-// gives row sums only.  Each tile's sums go to its own slot of `part`, and
-// y[i] adds its slots in a fixed tile order, so the result is the same on
-// every run.  n <= TRI_MAX_N; rows at or past ld4 are never read (the rows
-// n .. ld4 - 1 of the copy are zero).
-__device__ void cta_matvec_tri(const float* __restrict__ A, int n, int ld4, const float* xs, double* y64, float* y32,
-                               float* part) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int nt = (n + 31) >> 5;
-    const int ntiles = nt * (nt + 1) / 2;
-    __syncthreads();  // xs complete; part free
-    for (int t = warp; t < ntiles; t += nw) {
-        int bi = 0;
-        while ((bi + 1) * (bi + 2) / 2 <= t) ++bi;
-        const int bj = t - bi * (bi + 1) / 2;
-        const int c = bj * 32 + lane;
-        const int r0 = bi * 32;
-        const int rows = ld4 - r0 < 32 ? ld4 - r0 : 32;  // a multiple of 4
-        float a[32];
-#pragma unroll
-        for (int r = 0; r < 32; ++r) a[r] = 0.f;
-        if (c < n) {
-            const float4* col = reinterpret_cast<const float4*>(A + static_cast<int64_t>(c) * ld4 + r0);
-#pragma unroll
-            for (int k = 0; k < 8; ++k)
-                if (4 * k < rows) {
-                    const float4 v = __ldg(col + k);
-                    a[4 * k] = v.x;
-                    a[4 * k + 1] = v.y;
-                    a[4 * k + 2] = v.z;
-                    a[4 * k + 3] = v.w;
-                }
-        }
-        // Column sums (off-diagonal tiles): lane c, sum over the tile's rows.
-        if (bi != bj) {
-            float cs = 0.f;
-#pragma unroll
-            for (int r = 0; r < 32; ++r) cs = fmaf(a[r], (r0 + r < n) ? xs[r0 + r] : 0.f, cs);
-            part[t * 64 + 32 + lane] = cs;
-        }
-        // Row sums: a[r] * x_c summed over the lanes for each r, by recursive
-        // halving (after the step with offset o, lane l holds partial sums of
-        // the rows congruent to l modulo ... ); lane r ends with row r's sum.
-        const float xc = c < n ? xs[c] : 0.f;
-#pragma unroll
-        for (int r = 0; r < 32; ++r) a[r] *= xc;
-#pragma unroll
-        for (int o = 16; o >= 1; o >>= 1) {
-            const bool upper = (lane & o) != 0;
-#pragma unroll
-            for (int r = 0; r < o; ++r) {
-                // keep rows [r + o] when upper, rows [r] when lower; send the other half
-                const float send = upper ? a[r] : a[r + o];
-                const float keep = upper ? a[r + o] : a[r];
-                a[r] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-            }
-        }
-        part[t * 64 + lane] = a[0];
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int I = i >> 5, r = i & 31;
-        float s = 0.f;
-        for (int j = 0; j <= I; ++j) s += part[(I * (I + 1) / 2 + j) * 64 + r];           // tiles (I, j): rows
-        for (int k = I + 1; k < nt; ++k) s += part[(k * (k + 1) / 2 + I) * 64 + 32 + r];  // tiles (k, I): columns
-        if (y64) y64[i] = static_cast<double>(s);
-        if (y32) y32[i] = s;
-    }
-}
-
 // The matvec of a T-thread Lanczos CTA.
 template <int T>
 __device__ __forceinline__ void lz_matvec(const float* __restrict__ A, int n, int ld4, const float* xs, double* y64,
-                                          float* y32, float* part) {
+                                          float* y32) {
     if (T <= 128)
         cta_matvec_cols(A, n, ld4, xs, y64, y32);
-    else if (n > 128 && n <= TRI_MAX_N)
-        cta_matvec_tri(A, n, ld4, xs, y64, y32, part);
     else
         cta_matvec(A, n, ld4, xs, y64, y32);
 }
@@ -291,7 +203,6 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
     double* ry = y + ld4;
     float* x32 = reinterpret_cast<float*>(ry + ld4);  // ld4 floats
     float* u32 = x32 + ld4;
-    float* tpart = u32 + ld4;                          // tri_part_floats(n) floats
     const float* A = a32 + d.a32_off;
     double* V = vec + d.vec_off;
     double* alpha = V + static_cast<int64_t>(n) * m;
@@ -322,9 +233,9 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
     int nb = 0;
     for (int k = 0; k < m; ++k) {
         __syncthreads();
-        lz_matvec<T>(A, n, ld4, x32, nullptr, u32, tpart);  // u = A q
+        lz_matvec<T>(A, n, ld4, x32, nullptr, u32);  // u = A q
         __syncthreads();
-        lz_matvec<T>(A, n, ld4, u32, w, nullptr, tpart);    // w = A^T u
+        lz_matvec<T>(A, n, ld4, u32, w, nullptr);    // w = A^T u
         __syncthreads();
         double s = 0.0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) s += q[i] * w[i];
@@ -376,11 +287,11 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
     }
     __syncthreads();
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
-        lz_matvec<T>(A, n, ld4, x32, nullptr, u32, tpart);
+        lz_matvec<T>(A, n, ld4, x32, nullptr, u32);
         __syncthreads();
-        lz_matvec<T>(A, n, ld4, u32, ry, nullptr, tpart);
+        lz_matvec<T>(A, n, ld4, u32, ry, nullptr);
     } else {
-        lz_matvec<T>(A, n, ld4, x32, ry, nullptr, tpart);
+        lz_matvec<T>(A, n, ld4, x32, ry, nullptr);
     }
     __syncthreads();
     double s = 0.0;
@@ -699,8 +610,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         aoff += up_to(n * ld4, 64);
         voff += up_to(n * m + 8 * (m + 1), 32);
         const int c = lz_class(n);
-        b->lz_smem[c] = std::max<size_t>(b->lz_smem[c], 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float) +
-                                                            tri_part_floats(static_cast<int>(n)) * sizeof(float));
+        b->lz_smem[c] = std::max<size_t>(b->lz_smem[c], 5 * ld4 * sizeof(double) + 2 * ld4 * sizeof(float));
     }
     b->total_elems = xoff;
     // Lanczos launch order: blocks grouped by size class, largest class first.

@@ -199,21 +199,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         constexpr int SLICE = BN / (EW / 4);
         const int c_begin = ((warp - 2) / 4) * SLICE;
         int it = 0;
-        // The step epilogue's inputs are requested one tile ahead (the MMAs run
-        // up to ACC_BUFS tiles ahead, so the epilogue rarely waits for them).
-        if (blockIdx.x < num_tiles) {
-            const TileInfo t0 = tile_info(gw, ep, blockIdx.x);
-            prefetch_step_inputs(ep, t0, t0.bi * BM + q4 * 32, BN, c_begin, c_begin + SLICE);
-        }
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
             const int kb_total = tile_kblocks<KBE>(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
-            if (tile + static_cast<int>(gridDim.x) < num_tiles) {
-                const TileInfo tn = tile_info(gw, ep, tile + gridDim.x);
-                prefetch_step_inputs(ep, tn, tn.bi * BM + q4 * 32, BN, c_begin, c_begin + SLICE);
-            }
             if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {
                 record_error(err, abort_flag, DEVERR_EPI_WAIT);
                 break;
@@ -224,12 +214,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             const uint32_t tmem_row =
                 tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
             const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
-            if (ep.fmt == FMT_F16)
-                epilogue_tile<FMT_F16, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
-            else if (ep.fmt == FMT_F16Q8)
-                epilogue_tile<FMT_F16Q8, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
-            else
-                epilogue_tile<FMT_BF16, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
+            // The storage format follows the operands: F16Q8 for E4M3 products,
+            // BF16 for BF16 ones, FP16 otherwise (ep.fmt says the same), so
+            // each instantiation compiles one epilogue.
+            constexpr int FMT = FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16);
+            epilogue_tile<FMT, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -270,6 +259,10 @@ psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, in
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
     using Cfg = TcCfg<TERMS>;
     auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW, FP8>;
+    if (ep.kind != EPI_FINAL && ep.kind != EPI_FINAL32 && ep.fmt != (FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16))) {
+        set_error("gemm_tc: the epilogue's storage format does not match the operand type");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
     static bool configured = false;  // attribute set once per process (per instantiation)
     if (!configured) {
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));

@@ -260,10 +260,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
                 const uint32_t tmem_row =
                     tmem + (static_cast<uint32_t>(q4 * 32) << 16) + static_cast<uint32_t>(buf * ACC_SPLIT * BN);
                 const int nacc = kb_total < ACC_SPLIT ? kb_total : ACC_SPLIT;
-                if (ep.fmt == FMT_F16)
-                    epilogue_tile<FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
-                else
-                    epilogue_tile<FMT_BF16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
+                epilogue_tile<BF16 ? FMT_BF16 : FMT_F16, ACC_SPLIT>(ep, ti, tmem_row, p0, nacc);
             }
             tc_fence_before();
             __syncwarp();

@@ -328,25 +328,6 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
         store_run_diag<FMT>(ep.out, ld, rb, cb, p, q0, v);
 }
 
-// The step epilogue reads this warp's rows of A and A3 (columns c_begin ..
-// c_end of tile column bj, every 16-bit term plane).  Issued before the
-// accumulator is ready, these prefetches let the loads that follow find the
-// lines in L2 instead of waiting on DRAM; in a block-diagonal batch the
-// operands of all blocks are far larger than L2.
-__device__ __forceinline__ void prefetch_step_inputs(const EpiParams& ep, const TileInfo& ti, int64_t p0, int tn,
-                                                     int c_begin, int c_end) {
-    if (ep.kind != EPI_STEP) return;
-    const int64_t p = p0 + (threadIdx.x & 31);
-    if (ep.skip_pad && p >= ti.blk.n) return;  // padding rows: zero, skipped or unused
-    const int nt = ep.fmt == FMT_BF16 ? 3 : 2;
-    const size_t row = static_cast<size_t>(ti.blk.row_base + p) * ep.ld + ti.blk.col_base + ti.bj * tn + c_begin;
-    for (int t = 0; t < nt; ++t)
-        for (int c = 0; c < c_end - c_begin; c += 64) {  // 64 two-byte elements per 128-byte line
-            prefetch_l2(static_cast<const uint16_t*>(ep.A.term[t]) + row + c);
-            prefetch_l2(static_cast<const uint16_t*>(ep.A3.term[t]) + row + c);
-        }
-}
-
 // Epilogue of one tile for the warp whose first local row is p0 (lane = row
 // p0 + lane), reading the accumulators from TMEM, columns [c_begin, c_end)
 // of the tile.  TN is the tile width (the MMA's N): ti.bj counts column tiles
