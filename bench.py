@@ -527,6 +527,21 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
     scratch = pristine.clone()
     best = plan.autotune(scratch)
     info = plan.info()
+    tuned = plan.tuning()
+    # both routes for the blocks of n <= 128 (on chip / per-product launches), direct launches
+    routes = {}
+    if tuned["small_blocks"] > 0:
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for chip in (1, 0):
+            plan.configure(small_on_chip=chip)
+            plan.project(scratch)
+            ev0.record()
+            for _ in range(3):
+                plan.project(scratch)
+            ev1.record()
+            torch.cuda.synchronize()
+            routes["ms_small_on_chip" if chip else "ms_small_per_product"] = ev0.elapsed_time(ev1) / 3
+        plan.configure(small_on_chip=tuned["small_on_chip"])
     work = pristine.clone()
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
@@ -582,7 +597,8 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
             "dense_equiv_tflops": dense / (ms_batch / 1e3) / 1e12,
             "max_rel_diff_vs_one_call": max(diffs), "rel_frobenius_err_vs_evd_sample": evd,
             "autotune": {"best_ms": best, "acc_mode": info["acc_mode"], "tile_order": info["tile_order"],
-                         "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"]}}
+                         "small_on_chip": tuned["small_on_chip"], "small_blocks": tuned["small_blocks"],
+                         "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"], **routes}}
 
 
 # ---------------------------------------------------------------------------

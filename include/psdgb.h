@@ -288,9 +288,22 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * other (block b starts at element sum_{c<b} n_c^2), and projected in place —
  * the layout of a block-diagonal SDP iterate.  psdgb_batch_project is
  * asynchronous and allocates nothing (the plan owns its device memory), so
- * it can be captured in a CUDA graph.  psdgb_batch_autotune times every
- * accumulator configuration and tile order on the caller's scratch blocks
- * (overwritten) and keeps the fastest. */
+ * it can be captured in a CUDA graph.
+ *
+ * With FP16 / FP16x3 operands the blocks of n <= 128 (one 128 x 128 tile)
+ * can instead run their whole filter in one persistent kernel that keeps
+ * their three split matrices in shared memory ("small blocks on chip", the
+ * default for such plans); the per-product launches then take only the
+ * larger blocks.  Both routes give the same result bit for bit when the
+ * products use one accumulator per tile (acc_mode 2).
+ *
+ * psdgb_batch_autotune times every accumulator configuration, tile order and
+ * (where available) the on-chip route on the caller's scratch blocks
+ * (overwritten) and keeps the fastest.  psdgb_batch_configure sets them by
+ * hand (-1 keeps a setting; acc_mode 0..2, tile_order 0 (largest blocks
+ * first) or 1 (block order), small_on_chip 0 or 1 — 1 is refused for plans
+ * without such blocks); psdgb_batch_tuning reads them back, with the number
+ * of blocks the on-chip route would take. */
 typedef struct psdgb_batch psdgb_batch;
 psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
                                 psdgb_batch** out);
@@ -299,6 +312,9 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
                               int64_t* num_tiles, int* acc_mode, int* tile_order);
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
+psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip);
+psdgb_status psdgb_batch_tuning(const psdgb_batch* batch, int* acc_mode, int* tile_order, int* small_on_chip,
+                                int64_t* small_blocks);
 
 /* ---- eigenpairs and deflation ------------------------------------------------- */
 /* Replaces compute_eigenpairs (include/psd_projection/lanczos.h:19-44,

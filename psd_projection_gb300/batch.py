@@ -2,7 +2,8 @@
 
     plan = BatchPlan(sizes)                 # block sizes n_b
     plan.project(d_blocks)                  # packed column-major blocks, in place (async)
-    plan.autotune(scratch)                  # pick the fastest accumulator mode / tile order
+    plan.autotune(scratch)                  # pick the fastest accumulator mode / tile order / route
+    plan.configure(acc_mode=2, small_on_chip=0)   # or set them by hand
 
 `pack` / `unpack` convert between a list of square matrices and the packed layout.
 """
@@ -33,6 +34,11 @@ def _bind():
     lib.psdgb_batch_project.argtypes = [vp, vp, vp]
     lib.psdgb_batch_autotune.restype = c_int
     lib.psdgb_batch_autotune.argtypes = [vp, vp, vp, ctypes.POINTER(c_dbl)]
+    lib.psdgb_batch_configure.restype = c_int
+    lib.psdgb_batch_configure.argtypes = [vp, c_int, c_int, c_int]
+    lib.psdgb_batch_tuning.restype = c_int
+    lib.psdgb_batch_tuning.argtypes = [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                       ctypes.POINTER(c_i64)]
     _bound = True
     return lib
 
@@ -72,6 +78,18 @@ class BatchPlan:
                                              ctypes.byref(am), ctypes.byref(to)), "psdgb_batch_info")
         return {"total_elements": te.value, "device_bytes": db.value, "num_tiles": nt.value, "acc_mode": am.value,
                 "tile_order": to.value}
+
+    def configure(self, acc_mode: int = -1, tile_order: int = -1, small_on_chip: int = -1) -> None:
+        """Set the accumulator mode (0..2), tile order (0 largest first, 1 block
+        order) and the on-chip route for blocks of n <= 128 (0 / 1); -1 keeps."""
+        _capi.check(_bind().psdgb_batch_configure(self._h, acc_mode, tile_order, small_on_chip),
+                    "psdgb_batch_configure")
+
+    def tuning(self) -> dict:
+        am, to, oc, sb = c_int(), c_int(), c_int(), c_i64()
+        _capi.check(_bind().psdgb_batch_tuning(self._h, ctypes.byref(am), ctypes.byref(to), ctypes.byref(oc),
+                                               ctypes.byref(sb)), "psdgb_batch_tuning")
+        return {"acc_mode": am.value, "tile_order": to.value, "small_on_chip": oc.value, "small_blocks": sb.value}
 
     def project(self, d_blocks, stream=None) -> None:
         import torch

@@ -353,15 +353,17 @@ __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlock
                                                                    const BatchState* __restrict__ states,
                                                                    const float* __restrict__ a32,
                                                                    const double* __restrict__ x, int from_x,
-                                                                   SplitMat out, int fmt, int64_t ld) {
+                                                                   SplitMat out, int fmt, int64_t ld,
+                                                                   const int* __restrict__ idx) {
     static_assert(COPY_THREADS == 256, "two halves of 128 threads");
     __shared__ float sm[2][32][33];
-    const LzBlockDesc d = lz[blockIdx.x];
-    const BlockDesc bd = blocks[blockIdx.x];
+    const int bidx = idx ? idx[blockIdx.x] : static_cast<int>(blockIdx.x);  // idx: a subset of the blocks
+    const LzBlockDesc d = lz[bidx];
+    const BlockDesc bd = blocks[bidx];
     // The scaling runs in FP32 (as in the single-matrix split) and the FP64
     // input is narrowed on the integer ALUs (convert.h): FP64 instructions
     // issue slowly on this GPU.
-    const float inv = d2f_rn(states[blockIdx.x].inv_scale);
+    const float inv = d2f_rn(states[bidx].inv_scale);
     const int n = d.n, np = bd.np;
     const int h = threadIdx.x / 128, ht = threadIdx.x % 128;
     const int tx = ht % 32, ty0 = ht / 32;        // load phase: 32 x 4
@@ -438,9 +440,20 @@ struct psdgb_batch {
     int* lz_idx = nullptr;              // block indices grouped by Lanczos size class
     int64_t lz_start[LZ_CLASSES + 1] = {0, 0, 0, 0, 0};
     size_t lz_smem[LZ_CLASSES] = {0, 0, 0, 0};
+    // Blocks of n <= 128 (one 128 x 128 tile) with FP16-pair operands can run
+    // their whole chain on chip (batch_chain.cu); the grouped products then
+    // take only the larger blocks (tiles_big, split_idx_big).
+    bool chain_ok = false;
+    ChainBlock* chain = nullptr;
+    int chain_count = 0;
+    TileDesc* tiles_big[2] = {nullptr, nullptr};
+    int64_t num_tiles_big = 0;
+    int* split_idx_big = nullptr;
+    int64_t big_count = 0;
     // tuning
     int acc_mode = ACC_1X4;
     int order = 0;
+    int use_chain = 0;
 };
 
 namespace {
@@ -472,16 +485,25 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         count_launch();
         PSDGB_CUDA_TRY(cudaGetLastError());
     }
-    batch_split_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 0, b->A,
-                                                         b->fmt, b->ld);
+    const bool chain = b->use_chain && b->chain_ok;
+    float coeffs[64];
+    const int steps = psdgb_filter_coefficients(b->schedule, coeffs, 21);
+    if (chain) {
+        // The small blocks' whole filter, on chip; the rest below skips them.
+        PSDGB_TRY(launch_batch_chain(ds, b->precision, b->chain, b->chain_count, coeffs, steps, d_blocks, 0, s));
+        if (b->big_count == 0) return PSDGB_OK;
+    }
+    const dim3 split_grid(static_cast<unsigned>(chain ? b->big_count : count), COPY_SPLIT);
+    const int* split_idx = chain ? b->split_idx_big : nullptr;
+    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 0, b->A,
+                                                          b->fmt, b->ld, split_idx);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     PrecisionInfo pi{};
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
-    GroupWork gw{b->tiles[b->order], b->blocks, 0};
-    float coeffs[64];
-    const int steps = psdgb_filter_coefficients(b->schedule, coeffs, 21);
+    GroupWork gw{chain ? b->tiles_big[b->order] : b->tiles[b->order], b->blocks, 0};
+    const int64_t num_tiles = chain ? b->num_tiles_big : b->num_tiles;
     auto base = [&]() {
         EpiParams e{};
         e.fmt = b->fmt;
@@ -497,7 +519,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         EpiParams e1 = base();
         e1.kind = EPI_STORE;
         e1.out = b->A2;
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A, b->A, b->ld, b->rows, e1, gw, b->num_tiles, 0,
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A, b->A, b->ld, b->rows, e1, gw, num_tiles, 0,
                                 s));
         EpiParams e2 = base();
         e2.kind = EPI_STORE;
@@ -506,7 +528,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
             e2.dual = 1;
             e2.acc_scale = 0.5f;
         }
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, e2, gw, b->num_tiles,
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, e2, gw, num_tiles,
                                 0, s));
         EpiParams e3 = base();
         e3.kind = EPI_STEP;
@@ -520,11 +542,11 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
             e3.dual = 1;
             e3.acc_scale = 0.5f;
         }
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A3, b->A2, b->ld, b->rows, e3, gw, b->num_tiles,
+        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A3, b->A2, b->ld, b->rows, e3, gw, num_tiles,
                                 0, s));
     }
-    batch_split_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 1, b->A2,
-                                                         b->fmt, b->ld);
+    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 1, b->A2,
+                                                          b->fmt, b->ld, split_idx);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     EpiParams ef = base();
@@ -533,7 +555,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     ef.acc_scale = 0.5f;
     ef.x64 = d_blocks;
     ef.out64 = d_blocks;
-    return gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, b->num_tiles, 0, s);
+    return gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, num_tiles, 0, s);
 }
 
 }  // namespace
@@ -633,6 +655,26 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     std::stable_sort(tl_lpt.begin(), tl_lpt.end(),
                      [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });
     b->num_tiles = static_cast<int64_t>(tl_block.size());
+    // Small blocks (one 128 x 128 tile, n >= 1) for the on-chip chain with
+    // FP16-pair operands; the larger blocks' tile lists and split list.
+    b->chain_ok = precision == PSDGB_PREC_FP16X3 || precision == PSDGB_PREC_FP16;
+    std::vector<int> chain_idx, big_idx;
+    for (int64_t i = 0; i < count; ++i) {
+        if (b->chain_ok && bd[i].np == 128 && b->n[i] >= 1)
+            chain_idx.push_back(static_cast<int>(i));
+        else if (b->n[i] >= 1 || !b->chain_ok)
+            big_idx.push_back(static_cast<int>(i));
+    }
+    if (chain_idx.empty()) b->chain_ok = false;
+    std::vector<TileDesc> tb_block, tb_lpt;
+    for (const TileDesc& t : tl_block)
+        if (bd[t.block].np > 128) tb_block.push_back(t);
+    for (const TileDesc& t : tl_lpt)
+        if (bd[t.block].np > 128) tb_lpt.push_back(t);
+    b->num_tiles_big = static_cast<int64_t>(tb_block.size());
+    b->chain_count = static_cast<int>(chain_idx.size());
+    b->big_count = static_cast<int64_t>(big_idx.size());
+    b->use_chain = b->chain_ok ? 1 : 0;
     // Device memory: tables | states | FP32 copies | Lanczos vectors | operand planes.
     const size_t plane = static_cast<size_t>(b->rows) * b->ld * 2;
     const int nterms = format_terms(b->fmt);
@@ -645,7 +687,11 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_a32 = a256(sizeof(float) * std::max<int64_t>(aoff, 1));
     const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
     const size_t sz_ops = 3 * nterms * a256(plane);
-    b->dev_bytes = sz_blocks + sz_lz + sz_idx + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_ops;
+    const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1));
+    const size_t sz_tiles_big = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles_big, 1));
+    const size_t sz_big_idx = a256(sizeof(int) * std::max<size_t>(big_idx.size(), 1));
+    b->dev_bytes = sz_blocks + sz_lz + sz_idx + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain +
+                   2 * sz_tiles_big + sz_big_idx + sz_ops;
     cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -670,6 +716,14 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     p += sz_a32;
     b->vec = reinterpret_cast<double*>(p);
     p += sz_vec;
+    b->chain = reinterpret_cast<ChainBlock*>(p);
+    p += sz_chain;
+    b->tiles_big[0] = reinterpret_cast<TileDesc*>(p);
+    p += sz_tiles_big;
+    b->tiles_big[1] = reinterpret_cast<TileDesc*>(p);
+    p += sz_tiles_big;
+    b->split_idx_big = reinterpret_cast<int*>(p);
+    p += sz_big_idx;
     SplitMat* mats[3] = {&b->A, &b->A2, &b->A3};
     for (int mi = 0; mi < 3; ++mi)
         for (int t = 0; t < 3; ++t) {
@@ -687,6 +741,22 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
                                   cudaMemcpyHostToDevice));
         PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[1], tl_block.data(), sizeof(TileDesc) * b->num_tiles,
                                   cudaMemcpyHostToDevice));
+    }
+    if (b->num_tiles_big > 0) {
+        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles_big[0], tb_lpt.data(), sizeof(TileDesc) * b->num_tiles_big,
+                                  cudaMemcpyHostToDevice));
+        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles_big[1], tb_block.data(), sizeof(TileDesc) * b->num_tiles_big,
+                                  cudaMemcpyHostToDevice));
+    }
+    if (!big_idx.empty())
+        PSDGB_CUDA_TRY(cudaMemcpy(b->split_idx_big, big_idx.data(), sizeof(int) * big_idx.size(),
+                                  cudaMemcpyHostToDevice));
+    if (!chain_idx.empty()) {
+        std::vector<ChainBlock> cbs;
+        for (int i : chain_idx)
+            cbs.push_back(ChainBlock{b->a32 + lz[i].a32_off, lz[i].ld4, lz[i].n, lz[i].x_off, &b->states[i].scale,
+                                     &b->states[i].inv_scale});
+        PSDGB_CUDA_TRY(cudaMemcpy(b->chain, cbs.data(), sizeof(ChainBlock) * cbs.size(), cudaMemcpyHostToDevice));
     }
     // Padding rows/columns between blocks are never read; zero the planes once
     // so every TMA box reads finite values.
@@ -728,6 +798,35 @@ psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream)
     return batch_enqueue(b, d_blocks, static_cast<cudaStream_t>(stream));
 }
 
+psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip) {
+    if (!b || acc_mode < -1 || acc_mode > ACC_1X4 || tile_order < -1 || tile_order > 1 || small_on_chip < -1 ||
+        small_on_chip > 1) {
+        set_error("psdgb_batch_configure: bad arguments");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (small_on_chip == 1 && !b->chain_ok) {
+        set_error("psdgb_batch_configure: no blocks of n <= 128 with FP16 / FP16x3 operands to run on chip");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (acc_mode >= 0) b->acc_mode = acc_mode;
+    if (tile_order >= 0) b->order = tile_order;
+    if (small_on_chip >= 0) b->use_chain = small_on_chip;
+    return PSDGB_OK;
+}
+
+psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_order, int* small_on_chip,
+                                int64_t* small_blocks) {
+    if (!b) {
+        set_error("psdgb_batch_tuning: null batch");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (acc_mode) *acc_mode = b->acc_mode;
+    if (tile_order) *tile_order = b->order;
+    if (small_on_chip) *small_on_chip = b->use_chain && b->chain_ok ? 1 : 0;
+    if (small_blocks) *small_blocks = b->chain_ok ? b->chain_count : 0;
+    return PSDGB_OK;
+}
+
 psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void* stream, double* best_ms) {
     if (!b || (b->total_elems > 0 && !d_scratch_blocks)) {
         set_error("psdgb_batch_autotune: bad arguments");
@@ -739,28 +838,32 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     PSDGB_CUDA_TRY(cudaEventCreate(&e0));
     PSDGB_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_acc = b->acc_mode, best_order = b->order;
+    int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain;
     const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
-    for (int ai = 0; ai < 3; ++ai) {
-        for (int o = 0; o < 2; ++o) {
-            b->acc_mode = accs[ai];
-            b->order = o;
-            PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
-            PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
-            PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
-            PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
-            PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
-                best_acc = accs[ai];
-                best_order = o;
+    for (int ch = b->chain_ok ? 1 : 0; ch >= 0; --ch)
+        for (int ai = 0; ai < 3; ++ai) {
+            for (int o = 0; o < 2; ++o) {
+                b->acc_mode = accs[ai];
+                b->order = o;
+                b->use_chain = ch;
+                PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
+                PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
+                PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
+                PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
+                PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    best_acc = accs[ai];
+                    best_order = o;
+                    best_chain = ch;
+                }
             }
         }
-    }
     b->acc_mode = best_acc;
     b->order = best_order;
+    b->use_chain = best_chain;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms) *best_ms = best;

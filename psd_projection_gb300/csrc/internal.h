@@ -162,6 +162,23 @@ psdgb_status gemm_tc_group(DeviceState* ds, int precision, int acc_mode, const S
                            int64_t ld, int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_tiles,
                            int grid, cudaStream_t s);
 
+// ---- small blocks of a batch, whole chain on chip (batch_chain.cu) ---------------
+// One block of n <= 128 for batch_chain_kernel: its FP32 copy (rows of ld4
+// floats) and bound (scale = up or 1, and its inverse) from the batch's
+// Lanczos launch, and its offset in the packed FP64 blocks.
+struct ChainBlock {
+    const float* a32;
+    int ld4;
+    int n;
+    long long x_off;
+    const double* scale;
+    const double* inv_scale;
+};
+// The split, the steps' products and the final reconstruction of `count`
+// such blocks (FP16 / FP16x3), one persistent launch of `grid` CTAs (0: one per SM).
+psdgb_status launch_batch_chain(DeviceState* ds, int precision, const ChainBlock* d_blocks, int count,
+                                const float* coef, int steps, double* d_x, int grid, cudaStream_t s);
+
 // ---- Lanczos (lanczos.cu) ---------------------------------------------------------
 struct LanczosResult {
     double lo = 0.0, up = 1.0, theta = 0.0;

@@ -129,3 +129,91 @@ def test_batch_bf16x9_and_fp16():
         for x, y in zip(mats, got):
             proj, _ = rp.eig_psd(x)
             assert rp.rel_frobenius(y, proj) <= tol
+
+
+# Blocks of every size class around the 64 / 128 boundaries of the on-chip
+# route (one or two K blocks, one tile), an empty block, and larger blocks.
+ON_CHIP_SIZES = [0, 1, 2, 16, 33, 63, 64, 65, 100, 127, 128, 129, 200, 300, 5, 90, 256, 17]
+
+
+@pytest.mark.parametrize("prec_name,sched_name", [("fp16x3", "SCHEDULE_FP32"), ("fp16", "SCHEDULE_FP16")])
+def test_batch_small_blocks_on_chip_bit_identical(prec_name, sched_name):
+    """The on-chip route for blocks of n <= 128 (one persistent kernel, the
+    split matrices in shared memory) and the per-product launches give the
+    same result bit for bit with one accumulator per tile, in both tile
+    orders; each block within 1e-4 (fp16x3) / 2e-3 (fp16) of FP64 EVD."""
+    import torch
+
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    mats = _blocks(ON_CHIP_SIZES, seed=7)
+    pristine = pack(mats)
+    outs = {}
+    with BatchPlan(ON_CHIP_SIZES, psd.PRECISIONS[prec_name], getattr(psd, sched_name)) as plan:
+        t = plan.tuning()
+        assert t["small_blocks"] == sum(1 for n in ON_CHIP_SIZES if 1 <= n <= 128)
+        assert t["small_on_chip"] == 1
+        for order in (0, 1):
+            for chip in (1, 0):
+                plan.configure(acc_mode=2, tile_order=order, small_on_chip=chip)
+                d = pristine.clone()
+                plan.project(d)
+                torch.cuda.synchronize()
+                outs[(order, chip)] = d.cpu().numpy()
+    ref = outs[(0, 0)]
+    for key, v in outs.items():
+        assert np.array_equal(v, ref), key
+    tol = 1e-4 if prec_name == "fp16x3" else 2e-3
+    for n, x, y in zip(ON_CHIP_SIZES, mats, unpack(torch.from_numpy(ref), ON_CHIP_SIZES)):
+        if n >= 2:
+            proj, _ = rp.eig_psd(x)
+            assert rp.rel_frobenius(y, proj) <= tol, n
+
+
+def test_batch_only_small_blocks_and_graph():
+    """A batch of small blocks only (nothing left for the per-product
+    launches) on the on-chip route, direct and replayed from a CUDA graph."""
+    import torch
+
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    sizes = [1, 7, 64, 65, 128, 100, 40] * 40
+    mats = _blocks(sizes, seed=8)
+    pristine = pack(mats)
+    with BatchPlan(sizes) as plan:
+        assert plan.tuning()["small_on_chip"] == 1
+        direct = pristine.clone()
+        plan.project(direct)
+        work = pristine.clone()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            plan.project(work.clone(), stream=side)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            plan.project(work)
+        work.copy_(pristine)
+        g.replay()
+        torch.cuda.synchronize()
+    assert torch.equal(direct, work)
+    for n, x, y in zip(sizes[:7], mats[:7], unpack(direct, sizes)[:7]):
+        t = to_dev(x)
+        psd.composite_FP32_auto_scale(t)
+        assert rp.rel_frobenius(y, from_dev(t)) <= 1e-5 or np.linalg.norm(y) == 0.0, n
+
+
+def test_batch_on_chip_refused_without_fp16_pairs():
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan
+
+    with BatchPlan([64, 200], psd.PRECISIONS["bf16x9"], psd.SCHEDULE_FP32) as plan:
+        assert plan.tuning()["small_on_chip"] == 0
+        with pytest.raises(psd.PsdgbError, match="on chip"):
+            plan.configure(small_on_chip=1)
+        plan.configure(acc_mode=1, tile_order=1, small_on_chip=0)
+        t = plan.tuning()
+        assert (t["acc_mode"], t["tile_order"]) == (1, 1)
