@@ -340,66 +340,39 @@ __global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const
     }
 }
 
-// Operand terms of block b into the strided layout: from the FP32 copy
-// (from_x == 0) or the FP64 input (from_x != 0, upper triangle), times the
-// block's 1/up; zero in the padding of the block's np x np region.
-// Scaled operand terms of every block into the strided layout: from the
-// FP32 copy (from_x = 0, the first split) or from the caller's FP64 blocks
-// (from_x = 1, Xs = X / up).  The CTA walks pairs of 32 x 32 tiles of its
-// block's np x np area (zero outside n), one tile per half; each thread
-// writes 8 consecutive elements as one 16-byte store per term plane.
+// Scaled operand terms of every block into the strided layout, from the
+// FP32 copy: the first split A = X / up, and again Xs = X / up for the final
+// product (the copy holds exactly the FP32 narrowing of the symmetric matrix
+// X's upper triangle defines, which is what Xs needs).  The CTA walks the
+// 32 x 32 tiles of its block's np x np area (zero outside n), two at a time,
+// one per half; each thread writes 8 consecutive elements as one 16-byte
+// store per term plane.
 __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlockDesc* __restrict__ lz,
                                                                    const BlockDesc* __restrict__ blocks,
                                                                    const BatchState* __restrict__ states,
-                                                                   const float* __restrict__ a32,
-                                                                   const double* __restrict__ x, int from_x,
-                                                                   SplitMat out, int fmt, int64_t ld,
+                                                                   const float* __restrict__ a32, SplitMat out,
+                                                                   int fmt, int64_t ld,
                                                                    const int* __restrict__ idx) {
     static_assert(COPY_THREADS == 256, "two halves of 128 threads");
-    __shared__ float sm[2][32][33];
     const int bidx = idx ? idx[blockIdx.x] : static_cast<int>(blockIdx.x);  // idx: a subset of the blocks
     const LzBlockDesc d = lz[bidx];
     const BlockDesc bd = blocks[bidx];
-    // The scaling runs in FP32 (as in the single-matrix split) and the FP64
-    // input is narrowed on the integer ALUs (convert.h): FP64 instructions
-    // issue slowly on this GPU.
+    // The scaling runs in FP32, as in the single-matrix split.
     const float inv = d2f_rn(states[bidx].inv_scale);
     const int n = d.n, np = bd.np;
     const int h = threadIdx.x / 128, ht = threadIdx.x % 128;
-    const int tx = ht % 32, ty0 = ht / 32;        // load phase: 32 x 4
-    const int r = ht / 4, g = ht % 4;             // store phase: row r, columns 8g..8g+7
+    const int r = ht / 4, g = ht % 4;  // row r, columns 8g..8g+7 of the tile
     const int nt = np / 32;
     const int ntiles = nt * nt;
-    const double* X = x + d.x_off;
     const float* A = a32 + d.a32_off;
     const bool vec_ok = (d.ld4 % 4) == 0;
     for (int tp = blockIdx.y; 2 * tp < ntiles; tp += gridDim.y) {
         const int t = 2 * tp + h;
-        const bool valid = t < ntiles;
-        const int bi = valid ? t / nt : 0, bj = valid ? t % nt : 0;
-        if (from_x) {
-            const int rbase = (bi <= bj) ? bi * 32 : bj * 32;
-            const int cbase = (bi <= bj) ? bj * 32 : bi * 32;
-            __syncthreads();
-            for (int ty = ty0; ty < 32; ty += 4) {
-                const int rr = rbase + tx, c = cbase + ty;
-                sm[h][ty][tx] = (valid && rr < n && c < n) ? d2f_rn(X[rr + static_cast<int64_t>(c) * n]) : 0.0f;
-            }
-            __syncthreads();
-        }
-        if (!valid) continue;
+        if (t >= ntiles) continue;
+        const int bi = t / nt, bj = t % nt;
         const int i = bi * 32 + r, j0 = bj * 32 + 8 * g;
         float v[8];
-        if (from_x) {
-#pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const int cl = 8 * g + e;
-                float val = 0.0f;
-                if (i < n && j0 + e < n)
-                    val = (bi < bj) ? sm[h][cl][r] : (bi > bj) ? sm[h][r][cl] : ((r <= cl) ? sm[h][cl][r] : sm[h][r][cl]);
-                v[e] = val * inv;
-            }
-        } else if (vec_ok && i < n && j0 + 8 <= n) {
+        if (vec_ok && i < n && j0 + 8 <= n) {
             const float* src = A + static_cast<int64_t>(i) * d.ld4 + j0;
             const float4 u0 = *reinterpret_cast<const float4*>(src);
             const float4 u1 = *reinterpret_cast<const float4*>(src + 4);
@@ -445,11 +418,16 @@ struct psdgb_batch {
     // take only the larger blocks (tiles_big, split_idx_big).
     bool chain_ok = false;
     ChainBlock* chain = nullptr;
+    int* chain_next = nullptr;  // the chain kernel's work counter
     int chain_count = 0;
     TileDesc* tiles_big[2] = {nullptr, nullptr};
     int64_t num_tiles_big = 0;
     int* split_idx_big = nullptr;
     int64_t big_count = 0;
+    // The small blocks' bound and chain run on a second stream (high
+    // priority), forked from and joined back into the caller's stream.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // tuning
     int acc_mode = ACC_1X4;
     int order = 0;
@@ -466,37 +444,52 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     batch_to_f32_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, d_blocks, b->a32);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
-    for (int c = 0; c < LZ_CLASSES; ++c) {
+    // With the on-chip route, the blocks of n <= 128 (Lanczos classes 2 and
+    // 3, then the chain kernel) go to the side stream and overlap the larger
+    // blocks' latency-bound Lanczos launches; the two touch disjoint blocks.
+    const bool chain = b->use_chain && b->chain_ok;
+    if (chain) {
+        PSDGB_CUDA_TRY(cudaEventRecord(b->ev_fork, s));
+        PSDGB_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+    }
+    const int class_order[LZ_CLASSES] = {2, 3, 0, 1};  // the side stream's classes first
+    for (int ci = 0; ci < LZ_CLASSES; ++ci) {
+        const int c = class_order[ci];
         const int64_t cnt = b->lz_start[c + 1] - b->lz_start[c];
         if (cnt == 0) continue;
         const int* idx = b->lz_idx + b->lz_start[c];
         const unsigned g = static_cast<unsigned>(cnt);
         const size_t sm = b->lz_smem[c];
+        cudaStream_t ls = (chain && c >= 2) ? b->side : s;
         switch (c) {
-            case 0: lz_batch_kernel<512><<<g, 512, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+            case 0: lz_batch_kernel<512><<<g, 512, sm, ls>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
                                                             PSDGB_RESIDUAL_REFERENCE); break;
-            case 1: lz_batch_kernel<256><<<g, 256, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+            case 1: lz_batch_kernel<256><<<g, 256, sm, ls>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
                                                             PSDGB_RESIDUAL_REFERENCE); break;
-            case 2: lz_batch_kernel<128><<<g, 128, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+            case 2: lz_batch_kernel<128><<<g, 128, sm, ls>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
                                                             PSDGB_RESIDUAL_REFERENCE); break;
-            default: lz_batch_kernel<64><<<g, 64, sm, s>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
+            default: lz_batch_kernel<64><<<g, 64, sm, ls>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
                                                            PSDGB_RESIDUAL_REFERENCE); break;
         }
         count_launch();
         PSDGB_CUDA_TRY(cudaGetLastError());
     }
-    const bool chain = b->use_chain && b->chain_ok;
     float coeffs[64];
     const int steps = psdgb_filter_coefficients(b->schedule, coeffs, 21);
     if (chain) {
         // The small blocks' whole filter, on chip; the rest below skips them.
-        PSDGB_TRY(launch_batch_chain(ds, b->precision, b->chain, b->chain_count, coeffs, steps, d_blocks, 0, s));
-        if (b->big_count == 0) return PSDGB_OK;
+        PSDGB_TRY(launch_batch_chain(ds, b->precision, b->chain, b->chain_count, coeffs, steps, d_blocks,
+                                     b->chain_next, 0, b->side));
+        PSDGB_CUDA_TRY(cudaEventRecord(b->ev_join, b->side));
+        if (b->big_count == 0) {
+            PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
+            return PSDGB_OK;
+        }
     }
     const dim3 split_grid(static_cast<unsigned>(chain ? b->big_count : count), COPY_SPLIT);
     const int* split_idx = chain ? b->split_idx_big : nullptr;
-    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 0, b->A,
-                                                          b->fmt, b->ld, split_idx);
+    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A, b->fmt,
+                                                          b->ld, split_idx);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     PrecisionInfo pi{};
@@ -545,8 +538,8 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A3, b->A2, b->ld, b->rows, e3, gw, num_tiles,
                                 0, s));
     }
-    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, d_blocks, 1, b->A2,
-                                                          b->fmt, b->ld, split_idx);
+    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt,
+                                                          b->ld, split_idx);  // Xs
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     EpiParams ef = base();
@@ -555,7 +548,9 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     ef.acc_scale = 0.5f;
     ef.x64 = d_blocks;
     ef.out64 = d_blocks;
-    return gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, num_tiles, 0, s);
+    PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, num_tiles, 0, s));
+    if (chain) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
+    return PSDGB_OK;
 }
 
 }  // namespace
@@ -666,6 +661,8 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
             big_idx.push_back(static_cast<int>(i));
     }
     if (chain_idx.empty()) b->chain_ok = false;
+    // the chain kernel claims blocks in list order: largest first
+    std::stable_sort(chain_idx.begin(), chain_idx.end(), [&](int a, int c) { return b->n[a] > b->n[c]; });
     std::vector<TileDesc> tb_block, tb_lpt;
     for (const TileDesc& t : tl_block)
         if (bd[t.block].np > 128) tb_block.push_back(t);
@@ -687,7 +684,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_a32 = a256(sizeof(float) * std::max<int64_t>(aoff, 1));
     const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
     const size_t sz_ops = 3 * nterms * a256(plane);
-    const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1));
+    const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1)) + 256;
     const size_t sz_tiles_big = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles_big, 1));
     const size_t sz_big_idx = a256(sizeof(int) * std::max<size_t>(big_idx.size(), 1));
     b->dev_bytes = sz_blocks + sz_lz + sz_idx + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain +
@@ -717,6 +714,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     b->vec = reinterpret_cast<double*>(p);
     p += sz_vec;
     b->chain = reinterpret_cast<ChainBlock*>(p);
+    b->chain_next = reinterpret_cast<int*>(p + sz_chain - 256);
     p += sz_chain;
     b->tiles_big[0] = reinterpret_cast<TileDesc*>(p);
     p += sz_tiles_big;
@@ -751,6 +749,13 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     if (!big_idx.empty())
         PSDGB_CUDA_TRY(cudaMemcpy(b->split_idx_big, big_idx.data(), sizeof(int) * big_idx.size(),
                                   cudaMemcpyHostToDevice));
+    if (b->chain_ok) {
+        int least = 0, greatest = 0;
+        PSDGB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        PSDGB_CUDA_TRY(cudaStreamCreateWithPriority(&b->side, cudaStreamNonBlocking, greatest));
+        PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+        PSDGB_CUDA_TRY(cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming));
+    }
     if (!chain_idx.empty()) {
         std::vector<ChainBlock> cbs;
         for (int i : chain_idx)
@@ -774,6 +779,9 @@ psdgb_status psdgb_batch_destroy(psdgb_batch* b) {
     if (!b) return PSDGB_OK;
     cudaDeviceSynchronize();
     if (b->dev) cudaFree(b->dev);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+    if (b->ev_join) cudaEventDestroy(b->ev_join);
     delete b;
     return PSDGB_OK;
 }

@@ -50,8 +50,8 @@
 // matrices take their upper half from their lower half (warp shuffles);
 // matrices above the diagonal are not stored (their mirror is).  Thread 0
 // issues the MMAs.  One CTA per SM (199 KB of shared memory), persistent over
-// the list of small blocks, each block's inputs prefetched into L2 one block
-// ahead; every wait is bounded.
+// the list of small blocks (claimed from a counter, largest first), each
+// block's inputs prefetched into L2 one block ahead; every wait is bounded.
 #include <cuda.h>
 
 #include "convert.h"
@@ -170,6 +170,7 @@ struct ChainParams {
     int steps;
     int dual_steps;      // one-term products: the second and third products of a step take the symmetric part
     double* x;           // the batch's packed FP64 blocks (input, and output in place)
+    int* next;           // work counter (zero at launch): CTAs claim blocks in list order
     int* err;
 };
 
@@ -331,6 +332,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
     uint64_t* drain = bar + 1;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
     volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* claim = abort_flag + 1;  // [0] the block being run, [1] the next one (thread 0)
     const int warp = threadIdx.x / 32;
     if (threadIdx.x == 0) {
         mbar_init(bar, 1);
@@ -386,10 +388,23 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
             asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(xa), "r"(static_cast<uint32_t>(xb - xa))
                          : "memory");
     };
-    prefetch(blockIdx.x);
-    for (int bi = blockIdx.x; bi < cp.count && !stop; bi += gridDim.x) {
+    // Blocks are claimed from the counter one ahead (the list runs largest
+    // first), so CTAs that start late or draw small blocks take more.
+    if (threadIdx.x == 0) {
+        const int c0 = atomicAdd(cp.next, 1);
+        claim[0] = c0;
+        prefetch(c0);
+    }
+    __syncthreads();
+    for (;;) {
+        const int bi = claim[0];
+        if (bi >= cp.count || stop) break;
+        if (threadIdx.x == 0) {
+            const int c1 = atomicAdd(cp.next, 1);
+            claim[1] = c1;
+            prefetch(c1);
+        }
         const ChainBlock cb = cp.blocks[bi];
-        prefetch(bi + gridDim.x);
         kbh = cb.n > 64 ? 2 : 1;
         const int nr = (cb.n + 31) & ~31;
         const float inv = d2f_rn(*cb.inv_scale);
@@ -420,6 +435,8 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
         ch_epilogue(CH_FINAL, 0.5f * kF16AccUnscale, 0.f, 0.f, 0.f, nullptr, mA, mA3, dummy, tmem, cb, nr, cp.x);
         operands_ready();
         stop = *abort_flag != 0;
+        if (threadIdx.x == 0) claim[0] = claim[1];
+        __syncthreads();
     }
     // ---- teardown ----
     tc_fence_before();
@@ -438,7 +455,8 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
 }  // namespace
 
 psdgb_status launch_batch_chain(DeviceState* ds, int precision, const ChainBlock* d_blocks, int count,
-                                const float* coef, int steps, double* d_x, int grid, cudaStream_t s) {
+                                const float* coef, int steps, double* d_x, int* d_counter, int grid,
+                                cudaStream_t s) {
     if (count <= 0) return PSDGB_OK;
     if (steps > 16 || (precision != PSDGB_PREC_FP16X3 && precision != PSDGB_PREC_FP16)) {
         set_error("batch chain: FP16-pair precisions with at most 16 steps");
@@ -451,7 +469,9 @@ psdgb_status launch_batch_chain(DeviceState* ds, int precision, const ChainBlock
     cp.steps = steps;
     cp.dual_steps = precision == PSDGB_PREC_FP16 ? 1 : 0;
     cp.x = d_x;
+    cp.next = d_counter;
     cp.err = ds->d_error;
+    PSDGB_CUDA_TRY(cudaMemsetAsync(d_counter, 0, sizeof(int), s));
     int g = grid > 0 ? grid : sm_budget(ds);
     if (g > count) g = count;
     if (precision == PSDGB_PREC_FP16X3) {

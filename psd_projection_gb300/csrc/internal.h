@@ -175,9 +175,11 @@ struct ChainBlock {
     const double* inv_scale;
 };
 // The split, the steps' products and the final reconstruction of `count`
-// such blocks (FP16 / FP16x3), one persistent launch of `grid` CTAs (0: one per SM).
+// such blocks (FP16 / FP16x3), one persistent launch of `grid` CTAs (0: one
+// per SM) that claim blocks from *d_counter (reset on stream s first).
 psdgb_status launch_batch_chain(DeviceState* ds, int precision, const ChainBlock* d_blocks, int count,
-                                const float* coef, int steps, double* d_x, int grid, cudaStream_t s);
+                                const float* coef, int steps, double* d_x, int* d_counter, int grid,
+                                cudaStream_t s);
 
 // ---- Lanczos (lanczos.cu) ---------------------------------------------------------
 struct LanczosResult {
