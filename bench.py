@@ -528,20 +528,30 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
     best = plan.autotune(scratch)
     info = plan.info()
     tuned = plan.tuning()
-    # both routes for the blocks of n <= 128 (on chip / per-product launches), direct launches
+    # the alternatives the autotuner chose between, direct launches: the route of
+    # the blocks of n <= 128 (on chip / per-product launches) and the tile shape
+    # of the larger ones (256 x 256 pair tiles / 128 x 128 tiles only)
     routes = {}
-    if tuned["small_blocks"] > 0:
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        for chip in (1, 0):
-            plan.configure(small_on_chip=chip)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(**cfg):
+        plan.configure(**cfg)
+        plan.project(scratch)
+        ev0.record()
+        for _ in range(3):
             plan.project(scratch)
-            ev0.record()
-            for _ in range(3):
-                plan.project(scratch)
-            ev1.record()
-            torch.cuda.synchronize()
-            routes["ms_small_on_chip" if chip else "ms_small_per_product"] = ev0.elapsed_time(ev1) / 3
+        ev1.record()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / 3
+
+    if tuned["small_blocks"] > 0:
+        for chip in (1, 0):
+            routes["ms_small_on_chip" if chip else "ms_small_per_product"] = timed(small_on_chip=chip)
         plan.configure(small_on_chip=tuned["small_on_chip"])
+    if tuned["num_pair_tiles"] > 0:
+        for pairs in (1, 0):
+            routes["ms_pair_tiles" if pairs else "ms_single_tiles_only"] = timed(pair_tiles=pairs)
+        plan.configure(pair_tiles=tuned["pair_tiles"])
     work = pristine.clone()
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
@@ -598,6 +608,7 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
             "max_rel_diff_vs_one_call": max(diffs), "rel_frobenius_err_vs_evd_sample": evd,
             "autotune": {"best_ms": best, "acc_mode": info["acc_mode"], "tile_order": info["tile_order"],
                          "small_on_chip": tuned["small_on_chip"], "small_blocks": tuned["small_blocks"],
+                         "pair_tiles": tuned["pair_tiles"], "num_pair_tiles": tuned["num_pair_tiles"],
                          "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"], **routes}}
 
 

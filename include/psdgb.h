@@ -297,13 +297,20 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * larger blocks.  Both routes give the same result bit for bit when the
  * products use one accumulator per tile (acc_mode 2).
  *
- * psdgb_batch_autotune times every accumulator configuration, tile order and
- * (where available) the on-chip route on the caller's scratch blocks
- * (overwritten) and keeps the fastest.  psdgb_batch_configure sets them by
- * hand (-1 keeps a setting; acc_mode 0..2, tile_order 0 (largest blocks
- * first) or 1 (block order), small_on_chip 0 or 1 — 1 is refused for plans
- * without such blocks); psdgb_batch_tuning reads them back, with the number
- * of blocks the on-chip route would take. */
+ * Tile shape: the products of blocks of n > 128 run on 128 x 128 tiles, or
+ * (pair_tiles = 1, the default where the precision allows it) on 256 x 256
+ * tiles shared by a pair of SMs wherever two tile rows of a block fit (the
+ * odd last tile row of a block stays on 128 x 128 tiles): half the operand
+ * bytes per multiply-add.
+ *
+ * psdgb_batch_autotune times every tile shape, accumulator configuration,
+ * tile order and (where available) the on-chip route on the caller's scratch
+ * blocks (overwritten) and keeps the fastest.  psdgb_batch_configure sets
+ * them by hand (-1 keeps a setting; acc_mode 0..2, tile_order 0 (largest
+ * blocks first) or 1 (block order), small_on_chip 0 or 1, pair_tiles 0 or 1 —
+ * 1 is refused for plans without such blocks); psdgb_batch_tuning reads them
+ * back, with the number of blocks the on-chip route and of pair tiles the
+ * pair shape would take. */
 typedef struct psdgb_batch psdgb_batch;
 psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
                                 psdgb_batch** out);
@@ -312,9 +319,10 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
                               int64_t* num_tiles, int* acc_mode, int* tile_order);
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
-psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip);
+psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip,
+                                   int pair_tiles);
 psdgb_status psdgb_batch_tuning(const psdgb_batch* batch, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks);
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles);
 
 /* ---- eigenpairs and deflation ------------------------------------------------- */
 /* Replaces compute_eigenpairs (include/psd_projection/lanczos.h:19-44,

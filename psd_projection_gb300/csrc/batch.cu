@@ -3,8 +3,9 @@
 //
 // A block-diagonal SDP iterate is projected block by block; the reference
 // offers only one call per block (each a full chain of ~100 library calls).
-// Here the whole batch is one plan and ~35 kernel launches, independent of
-// the number of blocks, so it can be captured in one CUDA graph:
+// Here the whole batch is one plan and a fixed number of kernel launches,
+// independent of the number of blocks, so it can be captured in one CUDA
+// graph:
 //
 //   batch_to_f32      every block's upper triangle -> FP32 symmetric copy
 //   lz_batch_kernel   one CTA per block runs the whole Lanczos bound of its
@@ -12,17 +13,26 @@
 //                     and leaves the block's scale 1/up on the device; one
 //                     launch per size class (64 / 128 / 256 / 512 threads by
 //                     n), so small blocks run many CTAs per SM
-//   batch_split       scaled operand terms into one strided layout
-//   3 x steps         grouped persistent tensor-core products over the tile
-//                     list of all blocks (gemm_tc.cu)
-//   batch_split (X)   Xs = X / up per block
+//   batch_chain       (FP16 / FP16x3) the blocks of n <= 128: the whole filter
+//                     per block in one persistent kernel, operands in shared
+//                     memory (batch_chain.cu); these blocks' Lanczos classes
+//                     and this kernel run on a second stream, beside the
+//                     larger blocks' bound
+//   batch_split       scaled operand terms of the larger blocks into one
+//                     strided layout
+//   3 x steps         per product: 256 x 256 pair tiles (gemm_pairwide.cu)
+//                     and grouped 128 x 128 tiles (gemm_tc.cu) over the tile
+//                     lists of the larger blocks
+//   batch_split (Xs)  Xs = X / up per block
 //   1 dual product    (X + up (Xs A + A Xs)/2) / 2 into the caller's blocks
 //
 // Layout: blocks are padded to np = n rounded up to 128 and shelf-packed into
 // a strip of width ld = max np (blocks of one size side by side, a shelf per
 // row band), so a single TMA descriptor per operand plane covers every block.
-// The autotuner times the first product under each accumulator configuration
-// and tile order (LPT: largest K first, or block order) and keeps the fastest.
+// The autotuner times the whole projection under each tile shape (pair tiles
+// where two tile rows of a block fit, or 128 x 128 only), route of the small
+// blocks (on chip or per product), accumulator configuration and tile order
+// (LPT: largest blocks first, or block order) and keeps the fastest.
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -404,7 +414,16 @@ struct psdgb_batch {
     size_t dev_bytes = 0;
     BlockDesc* blocks = nullptr;
     LzBlockDesc* lz = nullptr;
-    TileDesc* tiles[2] = {nullptr, nullptr};  // 0: LPT order, 1: block order
+    // Product tile lists.  t128[route][shape][order]: the 128 x 128 tiles
+    // (route 1 leaves out the blocks of np = 128, which run on chip; shape 1
+    // leaves to the pair tiles every pair of tile rows that lies inside a
+    // block of np >= 256, keeping the odd last tile row); tpair[order]: those
+    // 256 x 256 pair tiles (shape 1).  order 0: largest blocks first (LPT),
+    // 1: block order.
+    TileDesc* t128[2][2][2] = {};
+    int64_t n128[2][2] = {};
+    TileDesc* tpair[2] = {nullptr, nullptr};
+    int64_t npair = 0;
     BatchState* states = nullptr;
     float* a32 = nullptr;
     double* vec = nullptr;
@@ -415,13 +434,11 @@ struct psdgb_batch {
     size_t lz_smem[LZ_CLASSES] = {0, 0, 0, 0};
     // Blocks of n <= 128 (one 128 x 128 tile) with FP16-pair operands can run
     // their whole chain on chip (batch_chain.cu); the grouped products then
-    // take only the larger blocks (tiles_big, split_idx_big).
+    // take only the larger blocks (t128[1], split_idx_big).
     bool chain_ok = false;
     ChainBlock* chain = nullptr;
     int* chain_next = nullptr;  // the chain kernel's work counter
     int chain_count = 0;
-    TileDesc* tiles_big[2] = {nullptr, nullptr};
-    int64_t num_tiles_big = 0;
     int* split_idx_big = nullptr;
     int64_t big_count = 0;
     // The small blocks' bound and chain run on a second stream (high
@@ -432,6 +449,8 @@ struct psdgb_batch {
     int acc_mode = ACC_1X4;
     int order = 0;
     int use_chain = 0;
+    int shape = 0;          // 1: pair tiles where they fit (pairs_ok)
+    bool pairs_ok = false;
 };
 
 namespace {
@@ -495,8 +514,19 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     PrecisionInfo pi{};
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
-    GroupWork gw{chain ? b->tiles_big[b->order] : b->tiles[b->order], b->blocks, 0};
-    const int64_t num_tiles = chain ? b->num_tiles_big : b->num_tiles;
+    const int route = chain ? 1 : 0, shape = (b->shape && b->pairs_ok) ? 1 : 0;
+    const GroupWork gw{b->t128[route][shape][b->order], b->blocks, 0};
+    const int64_t num_tiles = b->n128[route][shape];
+    const GroupWork gpw{b->tpair[b->order], b->blocks, 0};
+    const int64_t num_pairs = shape ? b->npair : 0;
+    // One product over the big blocks: the pair tiles, then the 128 x 128 tiles.
+    auto product = [&](const SplitMat& P, const SplitMat& Q, const EpiParams& e) -> psdgb_status {
+        if (num_pairs > 0)
+            PSDGB_TRY(gemm_tc_pairwide_group(ds, b->precision, P, Q, b->ld, b->rows, e, gpw, num_pairs, s));
+        if (num_tiles > 0)
+            PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, P, Q, b->ld, b->rows, e, gw, num_tiles, 0, s));
+        return PSDGB_OK;
+    };
     auto base = [&]() {
         EpiParams e{};
         e.fmt = b->fmt;
@@ -512,8 +542,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         EpiParams e1 = base();
         e1.kind = EPI_STORE;
         e1.out = b->A2;
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A, b->A, b->ld, b->rows, e1, gw, num_tiles, 0,
-                                s));
+        PSDGB_TRY(product(b->A, b->A, e1));
         EpiParams e2 = base();
         e2.kind = EPI_STORE;
         e2.out = b->A3;
@@ -521,8 +550,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
             e2.dual = 1;
             e2.acc_scale = 0.5f;
         }
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, e2, gw, num_tiles,
-                                0, s));
+        PSDGB_TRY(product(b->A2, b->A, e2));
         EpiParams e3 = base();
         e3.kind = EPI_STEP;
         e3.a = coeffs[3 * k];
@@ -535,8 +563,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
             e3.dual = 1;
             e3.acc_scale = 0.5f;
         }
-        PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A3, b->A2, b->ld, b->rows, e3, gw, num_tiles,
-                                0, s));
+        PSDGB_TRY(product(b->A3, b->A2, e3));
     }
     batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt,
                                                           b->ld, split_idx);  // Xs
@@ -548,7 +575,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     ef.acc_scale = 0.5f;
     ef.x64 = d_blocks;
     ef.out64 = d_blocks;
-    PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, b->A2, b->A, b->ld, b->rows, ef, gw, num_tiles, 0, s));
+    PSDGB_TRY(product(b->A2, b->A, ef));
     if (chain) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     return PSDGB_OK;
 }
@@ -639,17 +666,32 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
             if (lz_class(b->n[i]) == c) lz_order.push_back(static_cast<int>(i));
     }
     b->lz_start[LZ_CLASSES] = static_cast<int64_t>(lz_order.size());
-    // Tile lists: LPT (largest K first) and block order.
-    std::vector<TileDesc> tl_block;
+    // Tile lists (block order; the LPT order, largest blocks first, is made
+    // from it below).  Pair tiles (I, J), J <= I, cover tile rows 2I, 2I + 1
+    // of blocks of np >= 256 up to the last even tile row.
+    b->pairs_ok = pairwide_supported(precision);
+    std::vector<TileDesc> l128[2][2], lpair;
     for (int64_t i = 0; i < count; ++i) {
         const int nt = bd[i].np / 128;
-        for (int bi = 0; bi < nt; ++bi)
-            for (int bj = 0; bj <= bi; ++bj) tl_block.push_back(TileDesc{static_cast<int>(i), bi, bj, 0});
+        const int full_rows = (nt >= 2 && b->pairs_ok) ? 2 * (nt / 2) : 0;  // tile rows on pair tiles (shape 1)
+        for (int I = 0; I < full_rows / 2; ++I)
+            for (int J = 0; J <= I; ++J) lpair.push_back(TileDesc{static_cast<int>(i), I, J, 0});
+        for (int route = 0; route < 2; ++route) {
+            if (route == 1 && nt == 1) continue;  // on chip
+            for (int shape = 0; shape < 2; ++shape)
+                for (int bi = (shape ? full_rows : 0); bi < nt; ++bi)
+                    for (int bj = 0; bj <= bi; ++bj) l128[route][shape].push_back(TileDesc{static_cast<int>(i), bi, bj, 0});
+        }
     }
-    std::vector<TileDesc> tl_lpt = tl_block;
-    std::stable_sort(tl_lpt.begin(), tl_lpt.end(),
-                     [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });
-    b->num_tiles = static_cast<int64_t>(tl_block.size());
+    if (lpair.empty()) b->pairs_ok = false;
+    b->shape = b->pairs_ok ? 1 : 0;
+    auto lpt = [&](std::vector<TileDesc> v) {
+        std::stable_sort(v.begin(), v.end(),
+                         [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });
+        return v;
+    };
+    b->num_tiles = static_cast<int64_t>(l128[0][0].size());
+    b->npair = static_cast<int64_t>(lpair.size());
     // Small blocks (one 128 x 128 tile, n >= 1) for the on-chip chain with
     // FP16-pair operands; the larger blocks' tile lists and split list.
     b->chain_ok = precision == PSDGB_PREC_FP16X3 || precision == PSDGB_PREC_FP16;
@@ -663,12 +705,6 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     if (chain_idx.empty()) b->chain_ok = false;
     // the chain kernel claims blocks in list order: largest first
     std::stable_sort(chain_idx.begin(), chain_idx.end(), [&](int a, int c) { return b->n[a] > b->n[c]; });
-    std::vector<TileDesc> tb_block, tb_lpt;
-    for (const TileDesc& t : tl_block)
-        if (bd[t.block].np > 128) tb_block.push_back(t);
-    for (const TileDesc& t : tl_lpt)
-        if (bd[t.block].np > 128) tb_lpt.push_back(t);
-    b->num_tiles_big = static_cast<int64_t>(tb_block.size());
     b->chain_count = static_cast<int>(chain_idx.size());
     b->big_count = static_cast<int64_t>(big_idx.size());
     b->use_chain = b->chain_ok ? 1 : 0;
@@ -678,17 +714,20 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     auto a256 = [](size_t x) { return (x + 255) / 256 * 256; };
     const size_t sz_blocks = a256(sizeof(BlockDesc) * std::max<int64_t>(count, 1));
     const size_t sz_lz = a256(sizeof(LzBlockDesc) * std::max<int64_t>(count, 1));
-    const size_t sz_tiles = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles, 1));
+    // every tile list, both orders, one after the other
+    size_t tile_entries = 2 * lpair.size();
+    for (int r = 0; r < 2; ++r)
+        for (int sh = 0; sh < 2; ++sh) tile_entries += 2 * l128[r][sh].size();
+    const size_t sz_tiles = a256(sizeof(TileDesc) * std::max<size_t>(tile_entries, 1));
     const size_t sz_states = a256(sizeof(BatchState) * std::max<int64_t>(count, 1));
     const size_t sz_idx = a256(sizeof(int) * std::max<int64_t>(count, 1));
     const size_t sz_a32 = a256(sizeof(float) * std::max<int64_t>(aoff, 1));
     const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
     const size_t sz_ops = 3 * nterms * a256(plane);
     const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1)) + 256;
-    const size_t sz_tiles_big = a256(sizeof(TileDesc) * std::max<int64_t>(b->num_tiles_big, 1));
     const size_t sz_big_idx = a256(sizeof(int) * std::max<size_t>(big_idx.size(), 1));
-    b->dev_bytes = sz_blocks + sz_lz + sz_idx + 2 * sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain +
-                   2 * sz_tiles_big + sz_big_idx + sz_ops;
+    b->dev_bytes = sz_blocks + sz_lz + sz_idx + sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain + sz_big_idx +
+                   sz_ops;
     cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -703,9 +742,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     p += sz_lz;
     b->lz_idx = reinterpret_cast<int*>(p);
     p += sz_idx;
-    b->tiles[0] = reinterpret_cast<TileDesc*>(p);
-    p += sz_tiles;
-    b->tiles[1] = reinterpret_cast<TileDesc*>(p);
+    TileDesc* tile_store = reinterpret_cast<TileDesc*>(p);
     p += sz_tiles;
     b->states = reinterpret_cast<BatchState*>(p);
     p += sz_states;
@@ -716,10 +753,6 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     b->chain = reinterpret_cast<ChainBlock*>(p);
     b->chain_next = reinterpret_cast<int*>(p + sz_chain - 256);
     p += sz_chain;
-    b->tiles_big[0] = reinterpret_cast<TileDesc*>(p);
-    p += sz_tiles_big;
-    b->tiles_big[1] = reinterpret_cast<TileDesc*>(p);
-    p += sz_tiles_big;
     b->split_idx_big = reinterpret_cast<int*>(p);
     p += sz_big_idx;
     SplitMat* mats[3] = {&b->A, &b->A2, &b->A3};
@@ -734,17 +767,24 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         PSDGB_CUDA_TRY(cudaMemcpy(b->lz, lz.data(), sizeof(LzBlockDesc) * count, cudaMemcpyHostToDevice));
         PSDGB_CUDA_TRY(cudaMemcpy(b->lz_idx, lz_order.data(), sizeof(int) * count, cudaMemcpyHostToDevice));
     }
-    if (b->num_tiles > 0) {
-        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[0], tl_lpt.data(), sizeof(TileDesc) * b->num_tiles,
-                                  cudaMemcpyHostToDevice));
-        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles[1], tl_block.data(), sizeof(TileDesc) * b->num_tiles,
-                                  cudaMemcpyHostToDevice));
-    }
-    if (b->num_tiles_big > 0) {
-        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles_big[0], tb_lpt.data(), sizeof(TileDesc) * b->num_tiles_big,
-                                  cudaMemcpyHostToDevice));
-        PSDGB_CUDA_TRY(cudaMemcpy(b->tiles_big[1], tb_block.data(), sizeof(TileDesc) * b->num_tiles_big,
-                                  cudaMemcpyHostToDevice));
+    {
+        std::vector<TileDesc> all;
+        all.reserve(tile_entries);
+        auto place = [&](const std::vector<TileDesc>& v, TileDesc** out) {
+            const std::vector<TileDesc> l = lpt(v);
+            out[0] = tile_store + all.size();
+            all.insert(all.end(), l.begin(), l.end());
+            out[1] = tile_store + all.size();
+            all.insert(all.end(), v.begin(), v.end());
+        };
+        for (int r = 0; r < 2; ++r)
+            for (int sh = 0; sh < 2; ++sh) {
+                place(l128[r][sh], b->t128[r][sh]);
+                b->n128[r][sh] = static_cast<int64_t>(l128[r][sh].size());
+            }
+        place(lpair, b->tpair);
+        if (!all.empty())
+            PSDGB_CUDA_TRY(cudaMemcpy(tile_store, all.data(), sizeof(TileDesc) * all.size(), cudaMemcpyHostToDevice));
     }
     if (!big_idx.empty())
         PSDGB_CUDA_TRY(cudaMemcpy(b->split_idx_big, big_idx.data(), sizeof(int) * big_idx.size(),
@@ -806,9 +846,10 @@ psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream)
     return batch_enqueue(b, d_blocks, static_cast<cudaStream_t>(stream));
 }
 
-psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip) {
+psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip,
+                                   int pair_tiles) {
     if (!b || acc_mode < -1 || acc_mode > ACC_1X4 || tile_order < -1 || tile_order > 1 || small_on_chip < -1 ||
-        small_on_chip > 1) {
+        small_on_chip > 1 || pair_tiles < -1 || pair_tiles > 1) {
         set_error("psdgb_batch_configure: bad arguments");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
@@ -816,14 +857,19 @@ psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order,
         set_error("psdgb_batch_configure: no blocks of n <= 128 with FP16 / FP16x3 operands to run on chip");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
+    if (pair_tiles == 1 && !b->pairs_ok) {
+        set_error("psdgb_batch_configure: no blocks of n > 128 for 256 x 256 pair tiles at this precision");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
     if (acc_mode >= 0) b->acc_mode = acc_mode;
     if (tile_order >= 0) b->order = tile_order;
     if (small_on_chip >= 0) b->use_chain = small_on_chip;
+    if (pair_tiles >= 0) b->shape = pair_tiles;
     return PSDGB_OK;
 }
 
 psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks) {
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles) {
     if (!b) {
         set_error("psdgb_batch_tuning: null batch");
         return PSDGB_ERR_INVALID_ARGUMENT;
@@ -832,6 +878,8 @@ psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_o
     if (tile_order) *tile_order = b->order;
     if (small_on_chip) *small_on_chip = b->use_chain && b->chain_ok ? 1 : 0;
     if (small_blocks) *small_blocks = b->chain_ok ? b->chain_count : 0;
+    if (pair_tiles) *pair_tiles = b->shape && b->pairs_ok ? 1 : 0;
+    if (num_pair_tiles) *num_pair_tiles = b->pairs_ok ? b->npair : 0;
     return PSDGB_OK;
 }
 
@@ -846,32 +894,36 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     PSDGB_CUDA_TRY(cudaEventCreate(&e0));
     PSDGB_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain;
+    int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain, best_shape = b->shape;
     const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
-    for (int ch = b->chain_ok ? 1 : 0; ch >= 0; --ch)
-        for (int ai = 0; ai < 3; ++ai) {
-            for (int o = 0; o < 2; ++o) {
-                b->acc_mode = accs[ai];
-                b->order = o;
-                b->use_chain = ch;
-                PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
-                PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
-                PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
-                PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
-                PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
-                float ms = 0.f;
-                PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-                if (ms < best) {
-                    best = ms;
-                    best_acc = accs[ai];
-                    best_order = o;
-                    best_chain = ch;
+    for (int sh = b->pairs_ok ? 1 : 0; sh >= 0; --sh)
+        for (int ch = b->chain_ok ? 1 : 0; ch >= 0; --ch)
+            for (int ai = 0; ai < 3; ++ai) {
+                for (int o = 0; o < 2; ++o) {
+                    b->acc_mode = accs[ai];
+                    b->order = o;
+                    b->use_chain = ch;
+                    b->shape = sh;
+                    PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
+                    PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
+                    PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
+                    PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
+                    PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) {
+                        best = ms;
+                        best_acc = accs[ai];
+                        best_order = o;
+                        best_chain = ch;
+                        best_shape = sh;
+                    }
                 }
             }
-        }
     b->acc_mode = best_acc;
     b->order = best_order;
     b->use_chain = best_chain;
+    b->shape = best_shape;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms) *best_ms = best;

@@ -20,6 +20,11 @@
 // the accumulation is that of gemm_wide.cu (two TMEM slots of 256 columns,
 // K chunks drained into registers by 8 epilogue warps per CTA).  Every wait is
 // bounded; both CTAs meet at a cluster barrier before freeing TMEM or exiting.
+//
+// The same kernel serves a block-diagonal batch: with a device list of pair
+// tiles (block, I, J), the 256 x 256 tile I, J of that block (row I of pair
+// tiles is the block's tile rows 2I, 2I + 1, both inside the block), its
+// operands in the batch's strided layout and its K extent the block's n.
 #include "tc_kernel.cuh"
 
 namespace psdgb {
@@ -55,10 +60,42 @@ __device__ __forceinline__ uint64_t sdesc_pw(uint32_t saddr) {
         return sdesc_kmajor_sw64(saddr);
 }
 
-template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
+// Pair tile pt: from the batch's device list (gw.tiles), or the lower pair
+// tiles of the single matrix ep describes, in groups of group_rows pair rows.
+struct PwTile {
+    int64_t I, J;
+    BlockDesc blk;
+    int kb_half;  // K blocks of one product half
+};
+template <int KB, bool GROUP>
+__device__ __forceinline__ PwTile pw_tile(const GroupWork& gw, const EpiParams& ep, int pt, int group_rows) {
+    PwTile t;
+    if constexpr (GROUP) {
+        const TileDesc td = gw.tiles[pt];
+        t.I = td.bi;
+        t.J = td.bj;
+        t.blk = gw.blocks[td.block];
+        TileInfo ti;
+        ti.blk = t.blk;
+        t.kb_half = tile_kblocks<KB>(ep, ti);
+    } else {
+        const int64_t nsuper = (ep.np / BM + 1) / 2;  // pair rows / columns of 256
+        grouped_decode(pt, nsuper, group_rows, t.I, t.J);
+        t.blk.row_base = 0;
+        t.blk.np = static_cast<int>(ep.np);
+        t.blk.n = static_cast<int>(ep.n);
+        t.blk.col_base = 0;
+        t.blk.x_off = 0;
+        t.blk.up_dev = ep.up_dev;
+        t.kb_half = static_cast<int>(ep.np / KB);
+    }
+    return t;
+}
+
+template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB, bool GROUP>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
-    tc_pairwide_kernel(const __grid_constant__ TmapPW tm, const EpiParams ep, int group_rows, int num_pairs,
-                       int* err) {
+    tc_pairwide_kernel(const __grid_constant__ TmapPW tm, const EpiParams ep, const GroupWork gw, int group_rows,
+                       int num_pairs, int* err) {
     using Cfg = PairWideCfg<TERMS, KB>;
     constexpr int STAGES = Cfg::STAGES;
     constexpr int STAGE_BYTES = Cfg::STAGE_BYTES;
@@ -82,11 +119,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
     const uint32_t rank = cluster_ctarank();
     const bool leader = rank == 0;
     const int cluster = static_cast<int>(blockIdx.x >> 1), num_clusters = static_cast<int>(gridDim.x >> 1);
-    const int64_t nt = ep.np / BM;
-    const int64_t nsuper = (nt + 1) / 2;  // pair rows / columns of 256
-    const int kb_half = ep.np / KB;
-    const int kb_total = kb_half * (ep.dual ? 2 : 1);
-    const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
+    const int dual_mult = ep.dual ? 2 : 1;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
@@ -122,10 +155,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
         int g = 0;
         bool stop = false;
         for (int pt = cluster; pt < num_pairs && !stop; pt += num_clusters) {
-            int64_t I, J;
-            grouped_decode(pt, nsuper, group_rows, I, J);
-            const int row_a = static_cast<int>((2 * I + rank) * BM);
-            const int row_b = static_cast<int>((2 * J + rank) * BM);
+            const PwTile tl = pw_tile<KB, GROUP>(gw, ep, pt, group_rows);
+            const int kb_half = tl.kb_half;
+            const int kb_total = kb_half * dual_mult;
+            const int row_a = static_cast<int>(tl.blk.row_base + (2 * tl.I + rank) * BM);
+            const int row_b = static_cast<int>(tl.blk.row_base + (2 * tl.J + rank) * BM);
             for (int kb = 0; kb < kb_total; ++kb, ++g) {
                 const int s = g % STAGES;
                 const uint32_t ph = static_cast<uint32_t>(g / STAGES) & 1u;
@@ -142,7 +176,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
                 const bool second = kb >= kb_half;  // dual product: Q's rows against P's rows
                 const CUtensorMap* ma = second ? tm.Qa : tm.Pa;
                 const CUtensorMap* mb = second ? tm.Pa : tm.Qa;
-                const int kx = (second ? kb - kb_half : kb) * KB;
+                const int kx = tl.blk.col_base + (second ? kb - kb_half : kb) * KB;
                 if (leader) mbar_arrive_expect_tx(&full[s], 2 * STAGE_BYTES);
                 const uint32_t fb = full_leader + 8u * static_cast<uint32_t>(s);
 #pragma unroll
@@ -158,6 +192,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
         int g = 0, gc = 0;
         bool stop = false;
         for (int pt = cluster; pt < num_pairs && !stop; pt += num_clusters) {
+            const int kb_total = pw_tile<KB, GROUP>(gw, ep, pt, group_rows).kb_half * dual_mult;
+            const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
             for (int c = 0; c < nchunks; ++c, ++gc) {
                 const int slot = gc & 1;
                 const uint32_t use_ph = static_cast<uint32_t>(gc >> 1) & 1u;
@@ -208,17 +244,14 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
         int gc = 0;
         bool stop = false;
         for (int pt = cluster; pt < num_pairs && !stop; pt += num_clusters) {
-            int64_t I, J;
-            grouped_decode(pt, nsuper, group_rows, I, J);
+            const PwTile tl = pw_tile<KB, GROUP>(gw, ep, pt, group_rows);
+            const int kb_total = tl.kb_half * dual_mult;
+            const int nchunks = (kb_total + CHUNK - 1) / CHUNK;
+            const int64_t J = tl.J;
             TileInfo ti;
-            ti.bi = 2 * I + rank;
+            ti.bi = 2 * tl.I + rank;
             ti.bj = J;  // column tiles of 256
-            ti.blk.row_base = 0;
-            ti.blk.np = ep.np;
-            ti.blk.n = ep.n;
-            ti.blk.col_base = 0;
-            ti.blk.x_off = 0;
-            ti.blk.up_dev = ep.up_dev;
+            ti.blk = tl.blk;
             float sum[128];
             for (int c = 0; c < nchunks; ++c, ++gc) {
                 const int slot = gc & 1;
@@ -251,7 +284,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
                 __syncwarp();
                 if (lane == 0) mbar_arrive_cluster(acc_empty_leader + 8u * static_cast<uint32_t>(slot));
             }
-            if (stop || ti.bi >= nt) continue;
+            if (stop || ti.bi >= ti.blk.np / BM) continue;
             const int64_t p0 = ti.bi * BM + q4 * 32;
             const int64_t qbase = J * PW_N + half * 128;
 #pragma unroll
@@ -293,11 +326,13 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
     }
 }
 
-template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB>
-psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t np, const EpiParams& ep,
-                             cudaStream_t s) {
+// ld, rows: the operands' layout (np, np for a single matrix); gw: the
+// batch's pair-tile list (null tiles: the single matrix's lower pair tiles).
+template <int TERMS, int NPROD, bool BF16, int CHUNK, int KB, bool GROUP>
+psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
+                             const EpiParams& ep, const GroupWork& gw, int64_t num_pairs, cudaStream_t s) {
     using Cfg = PairWideCfg<TERMS, KB>;
-    auto kern = tc_pairwide_kernel<TERMS, NPROD, BF16, CHUNK, KB>;
+    auto kern = tc_pairwide_kernel<TERMS, NPROD, BF16, CHUNK, KB, GROUP>;
     static int max_clusters = 0;
     if (max_clusters == 0) {
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg::SMEM_BYTES));
@@ -324,18 +359,16 @@ psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat&
     for (int t = 0; t < 3; ++t) {
         void* pb = (t < TERMS) ? P.term[t] : P.term[0];
         void* qb = (t < TERMS) ? Q.term[t] : Q.term[0];
-        if (!make_tmap(&tm.Pa[t], pb, np, np, BF16, BM, KB) || !make_tmap(&tm.Qa[t], qb, np, np, BF16, BM, KB)) {
+        if (!make_tmap(&tm.Pa[t], pb, ld, rows, BF16, BM, KB) || !make_tmap(&tm.Qa[t], qb, ld, rows, BF16, BM, KB)) {
             set_error("cuTensorMapEncodeTiled failed");
             return PSDGB_ERR_CUDA;
         }
     }
-    const int64_t nsuper = (np / BM + 1) / 2;
-    const int64_t num_pairs = nsuper * (nsuper + 1) / 2;
     if (num_pairs <= 0) return PSDGB_OK;
     int clusters = num_pairs < max_clusters ? static_cast<int>(num_pairs) : max_clusters;
     if (clusters > sm_budget(ds) / 2) clusters = sm_budget(ds) / 2 > 0 ? sm_budget(ds) / 2 : 1;
     kern<<<static_cast<unsigned>(2 * clusters), PW_THREADS, Cfg::SMEM_BYTES, s>>>(
-        tm, ep, g_tile_group_rows, static_cast<int>(num_pairs), ds->d_error);
+        tm, ep, gw, g_tile_group_rows, static_cast<int>(num_pairs), ds->d_error);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     return PSDGB_OK;
@@ -346,27 +379,56 @@ psdgb_status launch_pairwide(DeviceState* ds, const SplitMat& P, const SplitMat&
 // One-, two- and three-term precisions.  Three BF16 terms take K blocks of 32
 // (64-byte swizzle): 48 KB stages, four of them in shared memory; chunks of
 // 32 K blocks (K = 1024) per TMEM slot, as for the others.
-psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
-                              const EpiParams& ep, cudaStream_t s) {
+namespace {
+
+template <bool GROUP>
+psdgb_status pairwide_dispatch(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t ld,
+                               int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_pairs,
+                               cudaStream_t s) {
     constexpr int WHOLE = 1 << 20;
     // K blocks of 64 (128-byte swizzle, 3 stages of 64 KB for two terms)
     // measured faster here than blocks of 32 (n = 8192, fp16x3: 1.87 vs 1.81
     // PFLOP/s); PSDGB_TUNE_WIDE_KBLOCK = 32 selects the latter.
     if (g_wide_kblock == 32 && (precision == PSDGB_PREC_FP16X3 || precision == PSDGB_PREC_BF16X3)) {
-        if (precision == PSDGB_PREC_FP16X3) return launch_pairwide<2, 3, false, 32, 32>(ds, P, Q, np, ep, s);
-        return launch_pairwide<2, 3, true, 32, 32>(ds, P, Q, np, ep, s);
+        if (precision == PSDGB_PREC_FP16X3)
+            return launch_pairwide<2, 3, false, 32, 32, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        return launch_pairwide<2, 3, true, 32, 32, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
     }
     switch (precision) {
-        case PSDGB_PREC_FP16: return launch_pairwide<1, 1, false, WHOLE, 64>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16: return launch_pairwide<1, 1, true, WHOLE, 64>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_FP16X3: return launch_pairwide<2, 3, false, 16, 64>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X3: return launch_pairwide<2, 3, true, 16, 64>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X6: return launch_pairwide<3, 6, true, 32, 32>(ds, P, Q, np, ep, s);
-        case PSDGB_PREC_BF16X9: return launch_pairwide<3, 9, true, 32, 32>(ds, P, Q, np, ep, s);
+        case PSDGB_PREC_FP16: return launch_pairwide<1, 1, false, WHOLE, 64, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        case PSDGB_PREC_BF16: return launch_pairwide<1, 1, true, WHOLE, 64, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        case PSDGB_PREC_FP16X3:
+            return launch_pairwide<2, 3, false, 16, 64, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        case PSDGB_PREC_BF16X3:
+            return launch_pairwide<2, 3, true, 16, 64, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        case PSDGB_PREC_BF16X6:
+            return launch_pairwide<3, 6, true, 32, 32, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
+        case PSDGB_PREC_BF16X9:
+            return launch_pairwide<3, 9, true, 32, 32, GROUP>(ds, P, Q, ld, rows, ep, gw, num_pairs, s);
         default: break;
     }
     set_error("gemm_tc_pairwide: precision not served by 256 x 256 pair tiles");
     return PSDGB_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+
+psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
+                              const EpiParams& ep, cudaStream_t s) {
+    const int64_t nsuper = (np / BM + 1) / 2;
+    const GroupWork none{nullptr, nullptr, 0};
+    return pairwide_dispatch<false>(ds, precision, P, Q, np, np, ep, none, nsuper * (nsuper + 1) / 2, s);
+}
+
+bool pairwide_supported(int precision) {
+    return precision == PSDGB_PREC_FP16 || precision == PSDGB_PREC_BF16 || precision == PSDGB_PREC_FP16X3 ||
+           precision == PSDGB_PREC_BF16X3 || precision == PSDGB_PREC_BF16X6 || precision == PSDGB_PREC_BF16X9;
+}
+
+psdgb_status gemm_tc_pairwide_group(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t ld,
+                                    int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_pairs,
+                                    cudaStream_t s) {
+    return pairwide_dispatch<true>(ds, precision, P, Q, ld, rows, ep, gw, num_pairs, s);
 }
 
 }  // namespace psdgb

@@ -153,6 +153,13 @@ psdgb_status gemm_tc_pair(DeviceState* ds, int precision, int acc_mode, const Sp
 // One matrix on CTA pairs with 256 x 256 tiles (gemm_pairwide.cu): one- and two-term precisions.
 psdgb_status gemm_tc_pairwide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                               const EpiParams& ep, cudaStream_t s);
+// The batch's pair tiles (TileDesc {block, I, J}: the 256 x 256 tile of tile
+// rows 2I, 2I + 1 against 2J, 2J + 1 of that block, both rows inside it) on
+// the same kernel; operands in the strided layout (ld, rows).
+bool pairwide_supported(int precision);
+psdgb_status gemm_tc_pairwide_group(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t ld,
+                                    int64_t rows, const EpiParams& ep, const GroupWork& gw, int64_t num_pairs,
+                                    cudaStream_t s);
 // One matrix on 128 x 256 tiles (gemm_wide.cu): one- and two-term precisions; np >= 256.
 psdgb_status gemm_tc_wide(DeviceState* ds, int precision, const SplitMat& P, const SplitMat& Q, int64_t np,
                           const EpiParams& ep, cudaStream_t s);

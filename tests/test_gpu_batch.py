@@ -217,3 +217,47 @@ def test_batch_on_chip_refused_without_fp16_pairs():
         plan.configure(acc_mode=1, tile_order=1, small_on_chip=0)
         t = plan.tuning()
         assert (t["acc_mode"], t["tile_order"]) == (1, 1)
+
+
+@pytest.mark.parametrize("prec_name,sched_name", [("fp16x3", "SCHEDULE_FP32"), ("bf16x9", "SCHEDULE_FP32")])
+def test_batch_pair_tiles_match_single_tiles(prec_name, sched_name):
+    """Blocks of n > 128 on 256 x 256 pair tiles (the odd last tile row of a
+    block on 128 x 128 tiles) against 128 x 128 tiles only, one accumulator
+    per tile: the same term products in the same K order, but a 256-wide MMA
+    on a CTA pair and a 128-wide one do not round their internal sums alike
+    (measured: 1.1-1.6e-6 relative apart at n = 600, below 1e-6 up to
+    n = 512), so the two agree to 5e-6 relative per block, below the
+    filter's own error against FP64 EVD (about 5e-6), and each shape gives
+    the same bits in both tile orders.  Each block within 1e-4 of FP64 EVD.
+    Sizes cover one, two, three, four and five tile rows."""
+    import torch
+
+    import psd_projection_gb300 as psd
+    from psd_projection_gb300.batch import BatchPlan, pack, unpack
+
+    sizes = [129, 200, 256, 257, 300, 384, 385, 512, 600, 640, 40, 100, 1, 0]
+    mats = _blocks(sizes, seed=9)
+    pristine = pack(mats)
+    outs = {}
+    with BatchPlan(sizes, psd.PRECISIONS[prec_name], getattr(psd, sched_name)) as plan:
+        t = plan.tuning()
+        # pair tiles per block: np 256 -> 1, 384 -> 1, 512 -> 3, 640 -> 3
+        assert t["pair_tiles"] == 1 and t["num_pair_tiles"] == 3 * 1 + 3 * 1 + 2 * 3 + 2 * 3
+        for order in (0, 1):
+            for pairs in (1, 0):
+                plan.configure(acc_mode=2, tile_order=order, pair_tiles=pairs)
+                d = pristine.clone()
+                plan.project(d)
+                torch.cuda.synchronize()
+                outs[(order, pairs)] = d.cpu().numpy()
+    for pairs in (0, 1):
+        assert np.array_equal(outs[(0, pairs)], outs[(1, pairs)]), pairs
+    single = unpack(torch.from_numpy(outs[(0, 0)]), sizes)
+    paired = unpack(torch.from_numpy(outs[(0, 1)]), sizes)
+    for n, x, y0, y1 in zip(sizes, mats, single, paired):
+        if n >= 2:
+            proj, _ = rp.eig_psd(x)
+            assert rp.rel_frobenius(y0, proj) <= 1e-4, n
+            assert rp.rel_frobenius(y1, proj) <= 1e-4, n
+            d = rp.rel_frobenius(y1, y0)
+            assert d <= 5e-6, (n, d)
