@@ -52,7 +52,7 @@ template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, 
 __global__ void __launch_bounds__(64 + 32 * EW, 1)
     tc_group_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, const GroupWork gw, int num_tiles,
                     int* err) {
-    using Cfg = TcCfg<TERMS>;
+    using Cfg = TcCfg<TERMS, EW * RUN_STAGE_BYTES>;
     // E4M3 operands (FP8 = true): 128 elements per 128-byte K block,
     // tcgen05.mma kind::f8f6f4 with K = 32 per instruction; the shared-memory
     // geometry in bytes is that of the 16-bit operands.
@@ -198,6 +198,8 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
         const int q4 = warp & 3;  // TMEM lane quarter this warp may access
         constexpr int SLICE = BN / (EW / 4);
         const int c_begin = ((warp - 2) / 4) * SLICE;
+        // this warp's staging buffer, after the barriers
+        uint8_t* stage = smem + STAGES * STAGE_BYTES + 512 + (warp - 2) * RUN_STAGE_BYTES;
         int it = 0;
         for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, ++it) {
             const TileInfo ti = tile_info(gw, ep, tile);
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             // BF16 for BF16 ones, FP16 otherwise (ep.fmt says the same), so
             // each instantiation compiles one epilogue.
             constexpr int FMT = FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16);
-            epilogue_tile<FMT, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE);
+            epilogue_tile<FMT, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE, stage);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -257,7 +259,7 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
 template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false>
 psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
-    using Cfg = TcCfg<TERMS>;
+    using Cfg = TcCfg<TERMS, EW * RUN_STAGE_BYTES>;
     auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW, FP8>;
     if (ep.kind != EPI_FINAL && ep.kind != EPI_FINAL32 && ep.fmt != (FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16))) {
         set_error("gemm_tc: the epilogue's storage format does not match the operand type");

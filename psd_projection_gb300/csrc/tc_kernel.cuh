@@ -33,15 +33,20 @@ constexpr int TILE_BYTES = BM * BK * 2;          // one operand term tile of 128
 constexpr int HALF_TILE_BYTES = TILE_BYTES / 2;  // 64 rows: one CTA's half of a pair's B operand
 
 // Single-CTA pipeline: per K block, TERMS term tiles of P (rows bi) and of Q
-// (rows bj); the ring takes as many stages as fit.
-template <int TERMS>
+// (rows bj); the ring takes as many stages as fit beside STAGING bytes of
+// epilogue staging (placed after the barriers).
+template <int TERMS, int STAGING = 0>
 struct TcCfg {
     static constexpr int STAGE_BYTES = 2 * TERMS * TILE_BYTES;
-    static constexpr int STAGES_FIT = (SMEM_LIMIT - 1024 /*align*/ - 512 /*barriers*/) / STAGE_BYTES;
+    static constexpr int STAGES_FIT = (SMEM_LIMIT - 1024 /*align*/ - 512 /*barriers*/ - STAGING) / STAGE_BYTES;
     static constexpr int STAGES = STAGES_FIT > 12 ? 12 : STAGES_FIT;
-    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;
+    static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512 + STAGING;
     static_assert(STAGES >= 2, "pipeline depth");
 };
+
+// Bytes of shared memory an epilogue warp stages one 32 x 32 run of one
+// 16-bit plane in (store_run_full_staged, store_run_diag_staged).
+constexpr int RUN_STAGE_BYTES = 32 * 64;
 
 struct TmapSet {
     CUtensorMap P[3];
@@ -213,6 +218,123 @@ __device__ __forceinline__ void store_run_full(const SplitMat& m, int64_t ld, in
     }
 }
 
+// Staging layout of a 32 x 32 run of one 16-bit plane: row r at r * 64
+// bytes, its 16-byte chunk c at chunk c ^ ((r >> 1) & 3), so that a lane
+// writing its own row and 8 lanes reading two rows are both free of bank
+// conflicts.
+__device__ __forceinline__ uint32_t stage_off(int r, int c) {
+    return static_cast<uint32_t>(r * 64 + ((c ^ ((r >> 1) & 3)) << 4));
+}
+
+// The staged run to global memory: rows row0 .. row0 + 31 (element index of
+// the run's first element, row stride ld), 8 rows x 64 bytes per warp
+// instruction (full 32-byte sectors) instead of 32 rows x 16 bytes.
+__device__ __forceinline__ void stage_flush(const uint8_t* stage, uint16_t* plane, size_t row0, int64_t ld) {
+    const int lane = threadIdx.x & 31;
+    const int c = lane & 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int r = 8 * j + (lane >> 2);
+        const uint4 w = *reinterpret_cast<const uint4*>(stage + stage_off(r, c));
+        *reinterpret_cast<uint4*>(plane + row0 + static_cast<size_t>(r) * ld + 8 * c) = w;
+    }
+}
+
+// The plane-t terms of the run's 32 values, two per word (element j in the
+// low half of word j / 2): the arithmetic of split_store.
+template <int FMT>
+__device__ __forceinline__ void split_plane(const float (&v)[32], int t, uint32_t (&pk)[16]) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 2) {
+        float x0 = v[j], x1 = v[j + 1];
+        if (FMT != FMT_BF16) {
+            x0 *= kF16Scale;
+            x1 *= kF16Scale;
+        }
+        uint16_t h0 = 0, h1 = 0;
+#pragma unroll
+        for (int u = 0; u <= t; ++u) {
+            if (FMT != FMT_BF16) {
+                const __half a0 = __float2half_rn(x0), a1 = __float2half_rn(x1);
+                h0 = __half_as_ushort(a0);
+                h1 = __half_as_ushort(a1);
+                x0 -= __half2float(a0);
+                x1 -= __half2float(a1);
+            } else {
+                const __nv_bfloat16 a0 = __float2bfloat16_rn(x0), a1 = __float2bfloat16_rn(x1);
+                h0 = __bfloat16_as_ushort(a0);
+                h1 = __bfloat16_as_ushort(a1);
+                x0 -= __bfloat162float(a0);
+                x1 -= __bfloat162float(a1);
+            }
+        }
+        pk[j / 2] = static_cast<uint32_t>(h0) | (static_cast<uint32_t>(h1) << 16);
+    }
+}
+
+// store_run_full with the rows through the warp's staging buffer (stage,
+// RUN_STAGE_BYTES): each lane writes its row's 64 bytes there, then the warp
+// writes whole row segments.  The mirror goes out as in store_run_full.  FP16
+// and BF16 formats.
+template <int FMT>
+__device__ __forceinline__ void store_run_full_staged(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb,
+                                                      int64_t p0, int64_t q0, const float (&v)[32], uint8_t* stage) {
+    constexpr int NT = FMT == FMT_BF16 ? 3 : 2;
+    const int lane = threadIdx.x & 31;
+    const size_t row0 = static_cast<size_t>(rb + p0) * ld + cb + q0;
+    const size_t mir_idx = static_cast<size_t>(rb + q0) * ld + cb + p0 + lane;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        uint32_t pk[16];
+        split_plane<FMT>(v, t, pk);
+        uint16_t* plane = static_cast<uint16_t*>(m.term[t]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            *reinterpret_cast<uint4*>(stage + stage_off(lane, u)) = make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
+        __syncwarp();
+        stage_flush(stage, plane, row0, ld);
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+            plane[mir_idx + static_cast<size_t>(j) * ld] = static_cast<uint16_t>(pk[j >> 1] >> ((j & 1) * 16));
+        __syncwarp();
+    }
+}
+
+// A run on the diagonal (q0 == p0 + its row offset 0) through the staging
+// buffer: every lane stages its whole row, the upper triangle (q > p) is
+// replaced by the mirror of the lower one in shared memory, and the whole
+// symmetric run goes out as row segments (it is its own mirror).  FP16 and
+// BF16 formats.
+template <int FMT>
+__device__ __forceinline__ void store_run_diag_staged(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb,
+                                                      int64_t p0, const float (&v)[32], uint8_t* stage) {
+    constexpr int NT = FMT == FMT_BF16 ? 3 : 2;
+    const int lane = threadIdx.x & 31;
+    const size_t row0 = static_cast<size_t>(rb + p0) * ld + cb + p0;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        uint32_t pk[16];
+        split_plane<FMT>(v, t, pk);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            *reinterpret_cast<uint4*>(stage + stage_off(lane, u)) = make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
+        __syncwarp();
+        // (lane, j) for j > lane takes (j, lane): a lower element of row j,
+        // which no lane writes here.
+#pragma unroll 4
+        for (int j = 1; j < 32; ++j) {
+            if (j > lane) {
+                const uint16_t h =
+                    *reinterpret_cast<const uint16_t*>(stage + stage_off(j, lane >> 3) + ((lane & 7) << 1));
+                *reinterpret_cast<uint16_t*>(stage + stage_off(lane, j >> 3) + ((j & 7) << 1)) = h;
+            }
+        }
+        __syncwarp();
+        stage_flush(stage, static_cast<uint16_t*>(m.term[t]), row0, ld);
+        __syncwarp();
+    }
+}
+
 // A run on the diagonal (q0 == p0): element-wise with the p >= q mask.
 template <int FMT>
 __device__ __forceinline__ void store_run_diag(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb, int64_t p,
@@ -264,9 +386,12 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
 // (p, q) and at the mirror (q, p).  FMT is the format the results are stored
 // in; E4M3_OPS says the product read the E4M3 plane (F16Q8 storage) rather
 // than the 16-bit terms.
+//
+// stage: the warp's RUN_STAGE_BYTES of shared memory for the staged stores,
+// or null for direct stores (the F16Q8 format always stores directly).
 template <int FMT, bool E4M3_OPS = false>
 __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo& ti, int64_t p0, int64_t q0,
-                                             float (&v)[32]) {
+                                             float (&v)[32], uint8_t* stage = nullptr) {
     const int64_t ld = ep.ld;
     const int64_t rb = ti.blk.row_base;
     const int64_t cb = ti.blk.col_base;
@@ -322,6 +447,13 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
             for (int j = 0; j < 8; ++j) v[8 * g + j] = fmaf(ep.c, v[8 * g + j], fmaf(ep.b, a3[j], ep.a * a[j]));
         }
     }
+    if (FMT != FMT_F16Q8 && stage != nullptr) {
+        if (q0 + 31 < p0)
+            store_run_full_staged<FMT>(ep.out, ld, rb, cb, p0, q0, v, stage);
+        else
+            store_run_diag_staged<FMT>(ep.out, ld, rb, cb, p0, v, stage);
+        return;
+    }
     if (q0 + 31 < p0)
         store_run_full<FMT>(ep.out, ld, rb, cb, p0, q0, v);
     else
@@ -334,7 +466,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
 // of TN, and the ACC_SPLIT accumulators of a tile sit TN TMEM columns apart.
 template <int FMT, int ACC_SPLIT, int TN = BN, bool E4M3_OPS = false>
 __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc,
-                              int c_begin = 0, int c_end = TN) {
+                              int c_begin = 0, int c_end = TN, uint8_t* stage = nullptr) {
     for (int c0 = c_begin; c0 < c_end; c0 += 32) {
         float v[32];
         tmem_ld_32cols(tmem_row + static_cast<uint32_t>(c0), v);
@@ -349,7 +481,7 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
         }
         const int64_t q0 = ti.bj * TN + c0;
         if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
-        epilogue_run<FMT, E4M3_OPS>(ep, ti, p0, q0, v);
+        epilogue_run<FMT, E4M3_OPS>(ep, ti, p0, q0, v, stage);
     }
 }
 
