@@ -44,9 +44,10 @@ struct TcCfg {
     static_assert(STAGES >= 2, "pipeline depth");
 };
 
-// Bytes of shared memory an epilogue warp stages one 32 x 32 run of one
-// 16-bit plane in (store_run_full_staged, store_run_diag_staged).
-constexpr int RUN_STAGE_BYTES = 32 * 64;
+// Bytes of shared memory an epilogue warp stages runs in: two 32 x 32 runs
+// of one 16-bit plane each (store_run_full_staged, store_run_diag_staged use
+// the first; the step epilogue's FP16 loads both).
+constexpr int RUN_STAGE_BYTES = 2 * 32 * 64;
 
 struct TmapSet {
     CUtensorMap P[3];
@@ -240,6 +241,52 @@ __device__ __forceinline__ void stage_flush(const uint8_t* stage, uint16_t* plan
     }
 }
 
+// Rows row0 .. row0 + 31 (32 elements each, row stride ld) of plane into the
+// staging buffer, as cp.async copies of 8 rows x 64 bytes per warp
+// instruction; the caller commits and waits.
+__device__ __forceinline__ void stage_fetch(const uint16_t* plane, size_t row0, int64_t ld, uint8_t* buf) {
+    const int lane = threadIdx.x & 31;
+    const int c = lane & 3;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int r = 8 * j + (lane >> 2);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(buf + stage_off(r, c))),
+                     "l"(plane + row0 + static_cast<size_t>(r) * ld + 8 * c)
+                     : "memory");
+    }
+}
+__device__ __forceinline__ void stage_fetch_wait() {
+    asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+    __syncwarp();
+}
+
+// The FP16-pair values of a run of matrix M (rows of row0, stride ld) for
+// this lane's row: both planes fetched coalesced through the staging buffer,
+// then lo + hi times 2^-12 (load_run8's arithmetic).
+__device__ __forceinline__ void stage_values_f16(const SplitMat& M, size_t row0, int64_t ld, uint8_t* stage,
+                                                 float (&out)[32]) {
+    const int lane = threadIdx.x & 31;
+    stage_fetch(static_cast<const uint16_t*>(M.term[0]), row0, ld, stage);
+    stage_fetch(static_cast<const uint16_t*>(M.term[1]), row0, ld, stage + 32 * 64);
+    stage_fetch_wait();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const uint4 h = *reinterpret_cast<const uint4*>(stage + stage_off(lane, u));
+        const uint4 l = *reinterpret_cast<const uint4*>(stage + 32 * 64 + stage_off(lane, u));
+        const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float l0 = __half2float(__ushort_as_half(static_cast<uint16_t>(lw[e] & 0xFFFFu)));
+            const float l1 = __half2float(__ushort_as_half(static_cast<uint16_t>(lw[e] >> 16)));
+            const float h0 = __half2float(__ushort_as_half(static_cast<uint16_t>(hw[e] & 0xFFFFu)));
+            const float h1 = __half2float(__ushort_as_half(static_cast<uint16_t>(hw[e] >> 16)));
+            out[8 * u + 2 * e] = ((0.f + l0) + h0) * kF16Unscale;
+            out[8 * u + 2 * e + 1] = ((0.f + l1) + h1) * kF16Unscale;
+        }
+    }
+    __syncwarp();
+}
+
 // The plane-t terms of the run's 32 values, two per word (element j in the
 // low half of word j / 2): the arithmetic of split_store.
 template <int FMT>
@@ -272,17 +319,17 @@ __device__ __forceinline__ void split_plane(const float (&v)[32], int t, uint32_
     }
 }
 
-// store_run_full with the rows through the warp's staging buffer (stage,
-// RUN_STAGE_BYTES): each lane writes its row's 64 bytes there, then the warp
-// writes whole row segments.  The mirror goes out as in store_run_full.  FP16
-// and BF16 formats.
+// store_run_full with the rows and the mirror through the warp's staging
+// buffer (stage, RUN_STAGE_BYTES): each lane writes its row's 64 bytes there
+// (then its column of the mirror, one 2-byte element per row), and the warp
+// writes whole row segments.  FP16 and BF16 formats.
 template <int FMT>
 __device__ __forceinline__ void store_run_full_staged(const SplitMat& m, int64_t ld, int64_t rb, int64_t cb,
                                                       int64_t p0, int64_t q0, const float (&v)[32], uint8_t* stage) {
     constexpr int NT = FMT == FMT_BF16 ? 3 : 2;
     const int lane = threadIdx.x & 31;
     const size_t row0 = static_cast<size_t>(rb + p0) * ld + cb + q0;
-    const size_t mir_idx = static_cast<size_t>(rb + q0) * ld + cb + p0 + lane;
+    const size_t mir0 = static_cast<size_t>(rb + q0) * ld + cb + p0;
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
         uint32_t pk[16];
@@ -293,9 +340,14 @@ __device__ __forceinline__ void store_run_full_staged(const SplitMat& m, int64_t
             *reinterpret_cast<uint4*>(stage + stage_off(lane, u)) = make_uint4(pk[4 * u], pk[4 * u + 1], pk[4 * u + 2], pk[4 * u + 3]);
         __syncwarp();
         stage_flush(stage, plane, row0, ld);
+        __syncwarp();
+        // mirror: element j of this lane's row goes to row j, column lane
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-            plane[mir_idx + static_cast<size_t>(j) * ld] = static_cast<uint16_t>(pk[j >> 1] >> ((j & 1) * 16));
+            *reinterpret_cast<uint16_t*>(stage + stage_off(j, lane >> 3) + ((lane & 7) << 1)) =
+                static_cast<uint16_t>(pk[j >> 1] >> ((j & 1) * 16));
+        __syncwarp();
+        stage_flush(stage, plane, mir0, ld);
         __syncwarp();
     }
 }
@@ -437,7 +489,19 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
     const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] *= acc_scale;
-    if (ep.kind == EPI_STEP) {
+    if (ep.kind == EPI_STEP && FMT == FMT_F16 && stage != nullptr) {
+        // A and A3 fetched coalesced through the staging buffer (same values
+        // and arithmetic as load_run8)
+        const size_t row0 = static_cast<size_t>(rb + p0) * ld + cb + q0;
+        float w[32];
+        stage_values_f16(ep.A, row0, ld, stage, w);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) w[j] *= ep.a;
+        float a3[32];
+        stage_values_f16(ep.A3, row0, ld, stage, a3);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) v[j] = fmaf(ep.c, v[j], fmaf(ep.b, a3[j], w[j]));
+    } else if (ep.kind == EPI_STEP) {
 #pragma unroll
         for (int g = 0; g < 4; ++g) {
             float a[8], a3[8];
