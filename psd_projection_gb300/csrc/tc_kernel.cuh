@@ -440,8 +440,10 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
 // than the 16-bit terms.
 //
 // stage: the warp's RUN_STAGE_BYTES of shared memory for the staged stores,
-// or null for direct stores (the F16Q8 format always stores directly).
-template <int FMT, bool E4M3_OPS = false>
+// or null for direct stores (the F16Q8 format always stores directly);
+// STAGED_LOADS: the FP16 step epilogue also fetches A and A3 through it (two
+// 32-value arrays more per thread: for callers with registers to spare).
+template <int FMT, bool E4M3_OPS = false, bool STAGED_LOADS = true>
 __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo& ti, int64_t p0, int64_t q0,
                                              float (&v)[32], uint8_t* stage = nullptr) {
     const int64_t ld = ep.ld;
@@ -489,7 +491,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
     const size_t idx = static_cast<size_t>(rb + p) * ld + cb + q0;
 #pragma unroll
     for (int j = 0; j < 32; ++j) v[j] *= acc_scale;
-    if (ep.kind == EPI_STEP && FMT == FMT_F16 && stage != nullptr) {
+    if (STAGED_LOADS && ep.kind == EPI_STEP && FMT == FMT_F16 && stage != nullptr) {
         // A and A3 fetched coalesced through the staging buffer (same values
         // and arithmetic as load_run8)
         const size_t row0 = static_cast<size_t>(rb + p0) * ld + cb + q0;
