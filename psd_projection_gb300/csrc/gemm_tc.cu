@@ -48,7 +48,8 @@ namespace {
 
 // ---- the kernel --------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false,
+          bool STAGED_FINAL = false>
 __global__ void __launch_bounds__(64 + 32 * EW, 1)
     tc_group_kernel(const __grid_constant__ TmapSet tm, const EpiParams ep, const GroupWork gw, int num_tiles,
                     int* err) {
@@ -220,7 +221,8 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             // BF16 for BF16 ones, FP16 otherwise (ep.fmt says the same), so
             // each instantiation compiles one epilogue.
             constexpr int FMT = FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16);
-            epilogue_tile<FMT, ACC_SPLIT, BN, FP8>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE, stage);
+            epilogue_tile<FMT, ACC_SPLIT, BN, FP8, STAGED_FINAL>(ep, ti, tmem_row, p0, nacc, c_begin, c_begin + SLICE,
+                                                                stage);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[buf]);
@@ -256,11 +258,12 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
 
 // ---- host side -------------------------------------------------------------
 
-template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false>
+template <int TERMS, int NPROD, bool BF16, int ACC_SPLIT, int ACC_BUFS, int EW, bool FP8 = false,
+          bool STAGED_FINAL = false>
 psdgb_status launch_tc(DeviceState* ds, const SplitMat& P, const SplitMat& Q, int64_t ld, int64_t rows,
                        const EpiParams& ep, const GroupWork& gw, int64_t num_tiles, int grid, cudaStream_t s) {
     using Cfg = TcCfg<TERMS, EW * RUN_STAGE_BYTES>;
-    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW, FP8>;
+    auto kern = tc_group_kernel<TERMS, NPROD, BF16, ACC_SPLIT, ACC_BUFS, EW, FP8, STAGED_FINAL>;
     if (ep.kind != EPI_FINAL && ep.kind != EPI_FINAL32 && ep.fmt != (FP8 ? FMT_F16Q8 : (BF16 ? FMT_BF16 : FMT_F16))) {
         set_error("gemm_tc: the epilogue's storage format does not match the operand type");
         return PSDGB_ERR_INVALID_ARGUMENT;
@@ -308,8 +311,15 @@ psdgb_status launch_acc(DeviceState* ds, int acc_mode, const SplitMat& P, const 
         case ACC_1X4:
             // Short-K tiles (block-diagonal batches, small matrices) are
             // epilogue-bound: twice the epilogue warps, each on half the columns.
-            if (g_group_epi_warps == 8)
+            if (g_group_epi_warps == 8) {
+                // the final reconstruction on its own instantiation, staged
+                if constexpr (!FP8) {
+                    if (ep.kind == EPI_FINAL)
+                        return launch_tc<TERMS, NPROD, BF16, 1, 4, 8, false, true>(ds, P, Q, ld, rows, ep, gw,
+                                                                                   num_tiles, grid, s);
+                }
                 return launch_tc<TERMS, NPROD, BF16, 1, 4, 8, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
+            }
             return launch_tc<TERMS, NPROD, BF16, 1, 4, 4, FP8>(ds, P, Q, ld, rows, ep, gw, num_tiles, grid, s);
         default: break;
     }

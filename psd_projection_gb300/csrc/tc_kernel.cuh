@@ -287,6 +287,62 @@ __device__ __forceinline__ void stage_values_f16(const SplitMat& M, size_t row0,
     __syncwarp();
 }
 
+// The final reconstruction of a run through the staging buffer, one half of
+// 16 columns at a time: X's run rows fetched into shared memory with
+// cp.async (8 bytes a lane, 16 lanes a row), each lane's o = (X + up acc) / 2
+// for its row, the rows written back as 128-byte row segments (the staged
+// value of element j of row r at double r * 16 + (j ^ (r & 15))); the mirror
+// goes out from each lane's own slots as 256-byte segments.  Same elements
+// (q <= p < n) and arithmetic as the direct path.
+__device__ __forceinline__ void final_run_staged(const EpiParams& ep, const TileInfo& ti, int64_t p0_, int64_t q0_,
+                                                 const float (&v)[32], float acc_scale, uint8_t* stage) {
+    // block-local row and column indices in 32 bits, element offsets in 64
+    const int lane = threadIdx.x & 31;
+    const int n = ti.blk.n, p0 = static_cast<int>(p0_), q0 = static_cast<int>(q0_);
+    if (p0 >= n) return;  // no row of the block (warp-uniform)
+    const double up = ti.blk.up_dev ? ep.up * *ti.blk.up_dev : ep.up;
+    double* out = ep.out64 + ti.blk.x_off;
+    const double* x = ep.x64 + ti.blk.x_off;
+    double* sd = reinterpret_cast<double*>(stage);
+    const int p = p0 + lane;
+    const int rsub = lane >> 4, j16 = lane & 15;  // fetch / flush mapping: rows 2 i + rsub, column j16
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int qh = q0 + 16 * h;
+        if (qh >= n) break;  // warp-uniform
+        const int q = qh + j16;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int r = 2 * i + rsub, pr = p0 + r;
+            if (q <= pr && pr < n && q < n)
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(sd + r * 16 + (j16 ^ (r & 15)))),
+                             "l"(x + static_cast<int64_t>(pr) * n + q)
+                             : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            double* slot = sd + lane * 16 + (j ^ (lane & 15));
+            if (qh + j <= p && p < n && qh + j < n)
+                *slot = 0.5 * (*slot + up * static_cast<double>(acc_scale * v[16 * h + j]));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int r = 2 * i + rsub, pr = p0 + r;
+            if (q <= pr && pr < n && q < n) out[static_cast<int64_t>(pr) * n + q] = sd[r * 16 + (j16 ^ (r & 15))];
+        }
+        // mirror: row qh + j, column p, for qh + j < p (the lane's own slots)
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int qj = qh + j;
+            if (qj < p && p < n && qj < n) out[static_cast<int64_t>(qj) * n + p] = sd[lane * 16 + (j ^ (lane & 15))];
+        }
+        __syncwarp();
+    }
+}
+
 // The plane-t terms of the run's 32 values, two per word (element j in the
 // low half of word j / 2): the arithmetic of split_store.
 template <int FMT>
@@ -442,8 +498,11 @@ __device__ __forceinline__ void load_run8(const SplitMat& m, size_t idx, float (
 // stage: the warp's RUN_STAGE_BYTES of shared memory for the staged stores,
 // or null for direct stores (the F16Q8 format always stores directly);
 // STAGED_LOADS: the FP16 step epilogue also fetches A and A3 through it (two
-// 32-value arrays more per thread: for callers with registers to spare).
-template <int FMT, bool E4M3_OPS = false, bool STAGED_LOADS = true>
+// 32-value arrays more per thread: for callers with registers to spare);
+// STAGED_FINAL: the final reconstruction goes through it too (its own kernel
+// instantiation: the staged final's registers would otherwise crowd the
+// product epilogues').
+template <int FMT, bool E4M3_OPS = false, bool STAGED_LOADS = true, bool STAGED_FINAL = false>
 __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo& ti, int64_t p0, int64_t q0,
                                              float (&v)[32], uint8_t* stage = nullptr) {
     const int64_t ld = ep.ld;
@@ -454,6 +513,10 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
     const float acc_scale = E4M3_OPS ? ep.acc_scale * kE4M3AccUnscale
                             : FMT != FMT_BF16 ? ep.acc_scale * kF16AccUnscale
                                               : ep.acc_scale;
+    if (STAGED_FINAL && ep.kind == EPI_FINAL && stage != nullptr) {
+        final_run_staged(ep, ti, p0, q0, v, acc_scale, stage);
+        return;
+    }
     if (ep.kind == EPI_FINAL) {
         const int64_t n = ti.blk.n;
         if (p >= n) return;
@@ -530,7 +593,7 @@ __device__ __forceinline__ void epilogue_run(const EpiParams& ep, const TileInfo
 // p0 + lane), reading the accumulators from TMEM, columns [c_begin, c_end)
 // of the tile.  TN is the tile width (the MMA's N): ti.bj counts column tiles
 // of TN, and the ACC_SPLIT accumulators of a tile sit TN TMEM columns apart.
-template <int FMT, int ACC_SPLIT, int TN = BN, bool E4M3_OPS = false>
+template <int FMT, int ACC_SPLIT, int TN = BN, bool E4M3_OPS = false, bool STAGED_FINAL = false>
 __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t tmem_row, int64_t p0, int nacc,
                               int c_begin = 0, int c_end = TN, uint8_t* stage = nullptr) {
     for (int c0 = c_begin; c0 < c_end; c0 += 32) {
@@ -547,7 +610,7 @@ __device__ void epilogue_tile(const EpiParams& ep, const TileInfo& ti, uint32_t 
         }
         const int64_t q0 = ti.bj * TN + c0;
         if (q0 > p0 + 31) continue;  // whole run above the diagonal: owned by the mirror tile
-        epilogue_run<FMT, E4M3_OPS>(ep, ti, p0, q0, v, stage);
+        epilogue_run<FMT, E4M3_OPS, true, STAGED_FINAL>(ep, ti, p0, q0, v, stage);
     }
 }
 
