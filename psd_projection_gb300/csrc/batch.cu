@@ -98,6 +98,30 @@ __device__ double cta_sum(double v, double* part, double* red) {
     return red[0];
 }
 
+// The square root r of a block-wide sum and 1 / r (r == 0: rinv = if_zero),
+// computed once by thread 0 and broadcast: an FP64 square root or division
+// is a sequence of FP64 instructions, which every warp issuing them would
+// queue on this part's scarce FP64 pipe.  IEEE-rounded either way, so the
+// same bits.
+__device__ void cta_sum_sqrt(double v, double* part, double* red, double if_zero, double& r, double& rinv) {
+    __syncthreads();
+    part[threadIdx.x] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = 0.0;
+        for (int i = threadIdx.x; i < static_cast<int>(blockDim.x); i += 32) t += part[i];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) {
+            const double s = sqrt(t);
+            red[0] = s;
+            red[1] = s != 0.0 ? 1.0 / s : if_zero;
+        }
+    }
+    __syncthreads();
+    r = red[0];
+    rinv = red[1];
+}
+
 // y[c] = sum_r A[c*ld4 + r] x[r] for the block's symmetric FP32 matrix.
 // Each warp takes four columns at a time and each lane keeps up to sixteen
 // float4 loads in flight (the columns are L2-resident and the loop is
@@ -129,7 +153,7 @@ __device__ void cta_matvec(const float* __restrict__ A, int n, int ld4, const fl
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
             const int c = c0 + j;
             if (lane == 0 && c < n) {
-                if (y64) y64[c] = static_cast<double>(acc);
+                if (y64) y64[c] = f2d(acc);  // exact, off the FP64 pipe
                 if (y32) y32[c] = acc;
             }
         }
@@ -171,7 +195,7 @@ __device__ void cta_matvec_cols(const float* __restrict__ A, int n, int ld4, con
             s3 = fmaf(a.w, xb.w, s3);
         }
         const float acc = (s0 + s1) + (s2 + s3);
-        if (y64) y64[c] = static_cast<double>(acc);
+        if (y64) y64[c] = f2d(acc);  // exact, off the FP64 pipe
         if (y32) y32[c] = acc;
     }
 }
@@ -231,13 +255,13 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
         q[i] = u;
         ss += u * u;
     }
-    const double nrm = sqrt(cta_sum(ss, part, red));
-    const double inv0 = nrm != 0.0 ? 1.0 / nrm : 1.0;
+    double nrm, inv0;
+    cta_sum_sqrt(ss, part, red, 1.0, nrm, inv0);
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         q[i] *= inv0;
         V[i] = q[i];
         vold[i] = 0.0;
-        x32[i] = static_cast<float>(q[i]);
+        x32[i] = d2f_rn(q[i]);
     }
     double beta_old = 0.0;
     int nb = 0;
@@ -256,18 +280,18 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
             w[i] = v;
             s += v * v;
         }
-        const double b = sqrt(cta_sum(s, part, red));
+        double b, binv;
+        cta_sum_sqrt(s, part, red, 0.0, b, binv);
         if (threadIdx.x == 0) {
             alpha[k] = a;
             beta[k] = b;
         }
         if ((b <= tol * a && k > 1) || b == 0.0) break;
-        const double binv = 1.0 / b;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const double qn = w[i] * binv;
             vold[i] = q[i];
             q[i] = qn;
-            x32[i] = static_cast<float>(qn);
+            x32[i] = d2f_rn(qn);
             if (k < m - 1) V[static_cast<int64_t>(k + 1) * n + i] = qn;
         }
         beta_old = b;
@@ -293,7 +317,7 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
         double s = 0.0;
         for (int j = 0; j < nb; ++j) s += V[static_cast<int64_t>(j) * n + i] * uk[j];
         y[i] = s;
-        x32[i] = static_cast<float>(s);
+        x32[i] = d2f_rn(s);
     }
     __syncthreads();
     if (residual_mode == PSDGB_RESIDUAL_EXACT) {
@@ -309,8 +333,9 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
         const double r = ry[i] - theta * y[i];
         s += r * r;
     }
-    const double rn = sqrt(cta_sum(s, part, red));
+    const double rs = cta_sum(s, part, red);
     if (threadIdx.x == 0) {
+        const double rn = sqrt(rs);
         const double up = sqrt(theta + rn);
         const double scale = up > 0.0 ? up : 1.0;
         *st = BatchState{theta, sqrt(theta), up, scale, 1.0 / scale, nb, 0};
@@ -684,7 +709,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         }
     }
     if (lpair.empty()) b->pairs_ok = false;
-    b->shape = b->pairs_ok ? 1 : 0;
+    b->shape = 0;  // 128 x 128 tiles until the autotuner or the caller picks pair tiles
     auto lpt = [&](std::vector<TileDesc> v) {
         std::stable_sort(v.begin(), v.end(),
                          [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });

@@ -44,6 +44,56 @@ PSDGB_HD float float_of_bits(uint32_t b) {
 #endif
 }
 
+PSDGB_HD uint32_t bits_of_float(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(x);
+#else
+    uint32_t b;
+    std::memcpy(&b, &x, sizeof b);
+    return b;
+#endif
+}
+
+PSDGB_HD double double_of_bits(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double(static_cast<long long>(b));
+#else
+    double d;
+    std::memcpy(&d, &b, sizeof d);
+    return d;
+#endif
+}
+
+PSDGB_HD int clz32(uint32_t x) {  // x != 0
+#if defined(__CUDA_ARCH__)
+    return __clz(static_cast<int>(x));
+#else
+    return __builtin_clz(x);
+#endif
+}
+
+// The binary32 value x as binary64, exactly (IEEE 754-2008, 5.4.2: every
+// binary32 number is a binary64 number): rebias the exponent and widen the
+// significand; a subnormal input is normalised; infinities carry over and
+// NaNs stay NaNs (quiet, payload kept).
+PSDGB_HD double f2d(float x) {
+    const uint32_t b = bits_of_float(x);
+    const uint64_t sign = static_cast<uint64_t>(b & 0x80000000u) << 32;
+    const int e32 = static_cast<int>((b >> 23) & 0xFF);
+    const uint32_t m = b & 0x007FFFFFu;
+    if (e32 == 0xFF)
+        return double_of_bits(sign | 0x7FF0000000000000ull | (static_cast<uint64_t>(m) << 29) |
+                              (m ? 0x0008000000000000ull : 0ull));
+    if (e32 != 0)
+        return double_of_bits(sign | (static_cast<uint64_t>(e32 - 127 + 1023) << 52) |
+                              (static_cast<uint64_t>(m) << 29));
+    if (m == 0) return double_of_bits(sign);
+    // m * 2^-149 with its top set bit at position t (0 .. 22): 1.f * 2^(t - 149)
+    const int t = 31 - clz32(m);
+    const uint64_t f = (static_cast<uint64_t>(m) << (52 - t)) & 0x000FFFFFFFFFFFFFull;
+    return double_of_bits(sign | (static_cast<uint64_t>(t - 149 + 1023) << 52) | f);
+}
+
 // Round the binary64 value x to the nearest binary32 value, ties to even.
 PSDGB_HD float d2f_rn(double x) {
     const uint64_t b = bits_of_double(x);

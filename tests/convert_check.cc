@@ -2,8 +2,9 @@
 // narrowing the copy and split kernels use) against the host compiler's own
 // conversion: random bit patterns, values across and below the binary32
 // range, exact ties and near-ties around every binary32 exponent, and the
-// special values.  Exit status 0 when every result has the same bits (NaN:
-// any NaN).
+// special values; and psdgb::f2d (the exact binary32 -> binary64 widening of
+// the batch Lanczos) on every binary32 bit pattern.  Exit status 0 when every
+// result has the same bits (NaN: any NaN).
 #include "convert.h"
 
 #include <cfloat>
@@ -13,6 +14,7 @@
 #include <random>
 
 using psdgb::d2f_rn;
+using psdgb::f2d;
 
 static unsigned bits(float f) {
     unsigned b;
@@ -52,6 +54,26 @@ int main() {
                                std::ldexp(1.0, -150), std::ldexp(1.0, -151), 1.0, -3.0, 1e300, -1e-300,
                                4.9406564584124654e-324};
     for (double s : specials) check(s);
+    // f2d: all 2^32 binary32 patterns, every 7th one (every exponent, both
+    // signs, subnormals, infinities, NaNs) plus the first and last 2^20
+    auto check_w = [&](unsigned b) {
+        float f;
+        std::memcpy(&f, &b, 4);
+        const double got = f2d(f), want = static_cast<double>(f);
+        unsigned long long gb, wb;
+        std::memcpy(&gb, &got, 8);
+        std::memcpy(&wb, &want, 8);
+        ++checked;
+        const bool ok = std::isnan(want) ? std::isnan(got) : gb == wb;
+        if (!ok && ++bad <= 10) std::printf("f2d mismatch at %08x: %a, expected %a\n", b, got, want);
+    };
+    for (unsigned long long b = 0; b < (1ull << 32); b += 7) check_w(static_cast<unsigned>(b));
+    for (unsigned b = 0; b < (1u << 20); ++b) {
+        check_w(b);
+        check_w(0x80000000u | b);
+        check_w(0x7F800000u - b);
+        check_w(0xFFFFFFFFu - b);
+    }
     std::printf("checked %ld values, %ld mismatches\n", checked, bad);
     return bad == 0 ? 0 : 1;
 }
