@@ -282,9 +282,9 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
 /* ---- block-diagonal batches ---------------------------------------------------
  * No counterpart in the reference, which projects one matrix per call.  A plan
  * for `count` symmetric blocks of the given sizes (0..4096) projects all of
- * them with ~35 kernel launches (independent of count): one CTA per block for
- * the Lanczos bound, one persistent tensor-core kernel per product over the
- * tiles of every block.  The blocks are packed column-major, one after the
+ * them with about 40 kernel launches (independent of count): one CTA per
+ * block for the Lanczos bound, one persistent tensor-core kernel per product
+ * over the tiles of every block.  The blocks are packed column-major, one after the
  * other (block b starts at element sum_{c<b} n_c^2), and projected in place —
  * the layout of a block-diagonal SDP iterate.  psdgb_batch_project is
  * asynchronous and allocates nothing (the plan owns its device memory), so
@@ -297,8 +297,8 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * larger blocks.  Both routes give the same result bit for bit when the
  * products use one accumulator per tile (acc_mode 2).
  *
- * Tile shape: the products of blocks of n > 128 run on 128 x 128 tiles, or
- * (pair_tiles = 1, the default where the precision allows it) on 256 x 256
+ * Tile shape: the products of blocks of n > 128 run on 128 x 128 tiles (the
+ * default), or (pair_tiles = 1, where the precision allows it) on 256 x 256
  * tiles shared by a pair of SMs wherever two tile rows of a block fit (the
  * odd last tile row of a block stays on 128 x 128 tiles): half the operand
  * bytes per multiply-add.
