@@ -475,6 +475,11 @@ struct psdgb_batch {
     int order = 0;
     int use_chain = 0;
     int shape = 0;          // 1: pair tiles where they fit (pairs_ok)
+    // With the on-chip route, the Lanczos classes from side_from on (2: the
+    // blocks of n <= 128; 1: also 128 < n <= 256, the caller's stream then
+    // joins the side stream before the larger blocks' products) run on the
+    // side stream.
+    int side_from = 2;
     bool pairs_ok = false;
 };
 
@@ -496,7 +501,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         PSDGB_CUDA_TRY(cudaEventRecord(b->ev_fork, s));
         PSDGB_CUDA_TRY(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
     }
-    const int class_order[LZ_CLASSES] = {2, 3, 0, 1};  // the side stream's classes first
+    const int class_order[LZ_CLASSES] = {1, 2, 3, 0};  // the side stream's classes first
     for (int ci = 0; ci < LZ_CLASSES; ++ci) {
         const int c = class_order[ci];
         const int64_t cnt = b->lz_start[c + 1] - b->lz_start[c];
@@ -504,7 +509,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         const int* idx = b->lz_idx + b->lz_start[c];
         const unsigned g = static_cast<unsigned>(cnt);
         const size_t sm = b->lz_smem[c];
-        cudaStream_t ls = (chain && c >= 2) ? b->side : s;
+        cudaStream_t ls = (chain && c >= b->side_from) ? b->side : s;
         switch (c) {
             case 0: lz_batch_kernel<512><<<g, 512, sm, ls>>>(b->lz, idx, b->a32, b->vec, b->states, b->tol, b->seed,
                                                             PSDGB_RESIDUAL_REFERENCE); break;
@@ -529,6 +534,8 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
             PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
             return PSDGB_OK;
         }
+        // the larger blocks' bound of class 1 ran on the side stream
+        if (b->side_from <= 1) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     }
     const dim3 split_grid(static_cast<unsigned>(chain ? b->big_count : count), COPY_SPLIT);
     const int* split_idx = chain ? b->split_idx_big : nullptr;
@@ -601,7 +608,7 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     ef.x64 = d_blocks;
     ef.out64 = d_blocks;
     PSDGB_TRY(product(b->A2, b->A, ef));
-    if (chain) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
+    if (chain && b->side_from > 1) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     return PSDGB_OK;
 }
 
@@ -919,15 +926,19 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     PSDGB_CUDA_TRY(cudaEventCreate(&e0));
     PSDGB_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
-    int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain, best_shape = b->shape;
+    int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain, best_shape = b->shape,
+        best_side = b->side_from;
     const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
+    // the route dimension: 0 per product; 2 / 1 on chip with the side stream
+    // taking the bound of n <= 128 / n <= 256
     for (int sh = b->pairs_ok ? 1 : 0; sh >= 0; --sh)
-        for (int ch = b->chain_ok ? 1 : 0; ch >= 0; --ch)
+        for (int rt = b->chain_ok ? 2 : 0; rt >= 0; --rt)
             for (int ai = 0; ai < 3; ++ai) {
                 for (int o = 0; o < 2; ++o) {
                     b->acc_mode = accs[ai];
                     b->order = o;
-                    b->use_chain = ch;
+                    b->use_chain = rt > 0 ? 1 : 0;
+                    b->side_from = rt == 1 ? 1 : 2;
                     b->shape = sh;
                     PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
                     PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
@@ -940,7 +951,8 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
                         best = ms;
                         best_acc = accs[ai];
                         best_order = o;
-                        best_chain = ch;
+                        best_chain = b->use_chain;
+                        best_side = b->side_from;
                         best_shape = sh;
                     }
                 }
@@ -948,6 +960,7 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     b->acc_mode = best_acc;
     b->order = best_order;
     b->use_chain = best_chain;
+    b->side_from = best_side;
     b->shape = best_shape;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
