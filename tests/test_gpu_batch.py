@@ -242,7 +242,7 @@ def test_batch_pair_tiles_match_single_tiles(prec_name, sched_name):
     with BatchPlan(sizes, psd.PRECISIONS[prec_name], getattr(psd, sched_name)) as plan:
         t = plan.tuning()
         # pair tiles per block: np 256 -> 1, 384 -> 1, 512 -> 3, 640 -> 3
-        assert t["pair_tiles"] == 1 and t["num_pair_tiles"] == 3 * 1 + 3 * 1 + 2 * 3 + 2 * 3
+        assert t["pair_tiles"] == 0 and t["num_pair_tiles"] == 3 * 1 + 3 * 1 + 2 * 3 + 2 * 3
         for order in (0, 1):
             for pairs in (1, 0):
                 plan.configure(acc_mode=2, tile_order=order, pair_tiles=pairs)
