@@ -288,7 +288,8 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * other (block b starts at element sum_{c<b} n_c^2), and projected in place —
  * the layout of a block-diagonal SDP iterate.  psdgb_batch_project is
  * asynchronous and allocates nothing (the plan owns its device memory), so
- * it can be captured in a CUDA graph.
+ * it can be captured in a CUDA graph; a plan serves one projection at a time
+ * (its operand buffers are per plan): make one plan per concurrent stream.
  *
  * With FP16 / FP16x3 operands the blocks of n <= 128 (one 128 x 128 tile)
  * can instead run their whole filter in one persistent kernel that keeps
