@@ -609,6 +609,7 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
             "autotune": {"best_ms": best, "acc_mode": info["acc_mode"], "tile_order": info["tile_order"],
                          "small_on_chip": tuned["small_on_chip"], "small_blocks": tuned["small_blocks"],
                          "pair_tiles": tuned["pair_tiles"], "num_pair_tiles": tuned["num_pair_tiles"],
+                         "serpentine": tuned["serpentine"],
                          "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"], **routes}}
 
 

@@ -304,14 +304,19 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * odd last tile row of a block stays on 128 x 128 tiles): half the operand
  * bytes per multiply-add.
  *
+ * Serpentine order (serpentine = 1): every other product walks its tile lists
+ * backwards, so that it starts on the blocks whose operands the product
+ * before it left in L2.
+ *
  * psdgb_batch_autotune times every tile shape, accumulator configuration,
- * tile order and (where available) the on-chip route on the caller's scratch
- * blocks (overwritten) and keeps the fastest.  psdgb_batch_configure sets
- * them by hand (-1 keeps a setting; acc_mode 0..2, tile_order 0 (largest
- * blocks first) or 1 (block order), small_on_chip 0 or 1, pair_tiles 0 or 1 —
- * 1 is refused for plans without such blocks); psdgb_batch_tuning reads them
- * back, with the number of blocks the on-chip route and of pair tiles the
- * pair shape would take. */
+ * tile order, serpentine order and (where available) the on-chip route on
+ * the caller's scratch blocks (overwritten) and keeps the fastest.
+ * psdgb_batch_configure sets them by hand (-1 keeps a setting; acc_mode
+ * 0..2, tile_order 0 (largest blocks first) or 1 (block order),
+ * small_on_chip, pair_tiles and serpentine 0 or 1 — small_on_chip or
+ * pair_tiles 1 is refused for plans without such blocks); psdgb_batch_tuning
+ * reads them back, with the number of blocks the on-chip route and of pair
+ * tiles the pair shape would take. */
 typedef struct psdgb_batch psdgb_batch;
 psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
                                 psdgb_batch** out);
@@ -321,9 +326,9 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
 psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip,
-                                   int pair_tiles);
+                                   int pair_tiles, int serpentine);
 psdgb_status psdgb_batch_tuning(const psdgb_batch* batch, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles);
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine);
 
 /* ---- eigenpairs and deflation ------------------------------------------------- */
 /* Replaces compute_eigenpairs (include/psd_projection/lanczos.h:19-44,

@@ -480,6 +480,9 @@ struct psdgb_batch {
     // joins the side stream before the larger blocks' products) run on the
     // side stream.
     int side_from = 2;
+    // Serpentine: every other product walks its tile lists backwards, so it
+    // starts on the blocks whose operands the product before left in L2.
+    int serpentine = 0;
     bool pairs_ok = false;
 };
 
@@ -547,15 +550,23 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
     const int route = chain ? 1 : 0, shape = (b->shape && b->pairs_ok) ? 1 : 0;
-    const GroupWork gw{b->t128[route][shape][b->order], b->blocks, 0};
+    GroupWork gw{b->t128[route][shape][b->order], b->blocks, 0};
     const int64_t num_tiles = b->n128[route][shape];
-    const GroupWork gpw{b->tpair[b->order], b->blocks, 0};
+    GroupWork gpw{b->tpair[b->order], b->blocks, 0};
     const int64_t num_pairs = shape ? b->npair : 0;
-    // One product over the big blocks: the pair tiles, then the 128 x 128 tiles.
+    int nprod = 0;
+    // One product over the big blocks: the pair tiles, then the 128 x 128
+    // tiles (with the serpentine order, every other product the other way
+    // round: its 128 x 128 tiles backwards first, then its pair tiles).
     auto product = [&](const SplitMat& P, const SplitMat& Q, const EpiParams& e) -> psdgb_status {
+        const bool back = b->serpentine && (nprod++ & 1);
+        gw.reverse = back ? static_cast<int>(num_tiles) : 0;
+        gpw.reverse = back ? static_cast<int>(num_pairs) : 0;
+        if (back && num_tiles > 0)
+            PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, P, Q, b->ld, b->rows, e, gw, num_tiles, 0, s));
         if (num_pairs > 0)
             PSDGB_TRY(gemm_tc_pairwide_group(ds, b->precision, P, Q, b->ld, b->rows, e, gpw, num_pairs, s));
-        if (num_tiles > 0)
+        if (!back && num_tiles > 0)
             PSDGB_TRY(gemm_tc_group(ds, b->precision, b->acc_mode, P, Q, b->ld, b->rows, e, gw, num_tiles, 0, s));
         return PSDGB_OK;
     };
@@ -879,9 +890,9 @@ psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream)
 }
 
 psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip,
-                                   int pair_tiles) {
+                                   int pair_tiles, int serpentine) {
     if (!b || acc_mode < -1 || acc_mode > ACC_1X4 || tile_order < -1 || tile_order > 1 || small_on_chip < -1 ||
-        small_on_chip > 1 || pair_tiles < -1 || pair_tiles > 1) {
+        small_on_chip > 1 || pair_tiles < -1 || pair_tiles > 1 || serpentine < -1 || serpentine > 1) {
         set_error("psdgb_batch_configure: bad arguments");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
@@ -897,11 +908,12 @@ psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order,
     if (tile_order >= 0) b->order = tile_order;
     if (small_on_chip >= 0) b->use_chain = small_on_chip;
     if (pair_tiles >= 0) b->shape = pair_tiles;
+    if (serpentine >= 0) b->serpentine = serpentine;
     return PSDGB_OK;
 }
 
 psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles) {
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine) {
     if (!b) {
         set_error("psdgb_batch_tuning: null batch");
         return PSDGB_ERR_INVALID_ARGUMENT;
@@ -912,6 +924,7 @@ psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_o
     if (small_blocks) *small_blocks = b->chain_ok ? b->chain_count : 0;
     if (pair_tiles) *pair_tiles = b->shape && b->pairs_ok ? 1 : 0;
     if (num_pair_tiles) *num_pair_tiles = b->pairs_ok ? b->npair : 0;
+    if (serpentine) *serpentine = b->serpentine;
     return PSDGB_OK;
 }
 
@@ -927,41 +940,52 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     PSDGB_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain, best_shape = b->shape,
-        best_side = b->side_from;
+        best_side = b->side_from, best_serp = b->serpentine;
     const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
-    // the route dimension: 0 per product; 2 / 1 on chip with the side stream
-    // taking the bound of n <= 128 / n <= 256
-    for (int sh = b->pairs_ok ? 1 : 0; sh >= 0; --sh)
-        for (int rt = b->chain_ok ? 2 : 0; rt >= 0; --rt)
-            for (int ai = 0; ai < 3; ++ai) {
-                for (int o = 0; o < 2; ++o) {
-                    b->acc_mode = accs[ai];
-                    b->order = o;
-                    b->use_chain = rt > 0 ? 1 : 0;
-                    b->side_from = rt == 1 ? 1 : 2;
-                    b->shape = sh;
-                    PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
-                    PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
-                    PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
-                    PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
-                    PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
-                    float ms = 0.f;
-                    PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-                    if (ms < best) {
-                        best = ms;
-                        best_acc = accs[ai];
-                        best_order = o;
-                        best_chain = b->use_chain;
-                        best_side = b->side_from;
-                        best_shape = sh;
-                    }
-                }
-            }
+    // Every combination of: serpentine order (off, on), tile shape (128 x 128;
+    // pair tiles where available), small-block route (per product; on chip
+    // with the side stream taking the bound of n <= 128, or of n <= 256),
+    // accumulator configuration (3) and tile order (LPT, block order).
+    const int nsh = b->pairs_ok ? 2 : 1, nrt = b->chain_ok ? 3 : 1;
+    for (int cfg = 0; cfg < 2 * nsh * nrt * 3 * 2; ++cfg) {
+        int c = cfg;
+        const int o = c % 2;
+        c /= 2;
+        const int ai = c % 3;
+        c /= 3;
+        const int rt = c % nrt;
+        c /= nrt;
+        const int sh = c % nsh;
+        const int sp = c / nsh;
+        b->acc_mode = accs[ai];
+        b->order = o;
+        b->use_chain = rt > 0 ? 1 : 0;
+        b->side_from = rt == 2 ? 1 : 2;
+        b->shape = sh;
+        b->serpentine = sp;
+        PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
+        PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
+        PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
+        PSDGB_CUDA_TRY(cudaEventRecord(e1, s));
+        PSDGB_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        PSDGB_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+            best = ms;
+            best_acc = accs[ai];
+            best_order = o;
+            best_chain = b->use_chain;
+            best_side = b->side_from;
+            best_shape = sh;
+            best_serp = sp;
+        }
+    }
     b->acc_mode = best_acc;
     b->order = best_order;
     b->use_chain = best_chain;
     b->side_from = best_side;
     b->shape = best_shape;
+    b->serpentine = best_serp;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms) *best_ms = best;

@@ -214,6 +214,7 @@ struct GroupWork {
     const TileDesc* tiles;
     const BlockDesc* blocks;
     int group_rows;  // implicit list only: tile order in groups of this many tile rows (0: row by row)
+    int reverse = 0; // device tables only: nonzero = the list's length, walked from its end
 };
 
 // ---------------------------------------------------------------------------

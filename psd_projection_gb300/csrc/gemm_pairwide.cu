@@ -71,7 +71,7 @@ template <int KB, bool GROUP>
 __device__ __forceinline__ PwTile pw_tile(const GroupWork& gw, const EpiParams& ep, int pt, int group_rows) {
     PwTile t;
     if constexpr (GROUP) {
-        const TileDesc td = gw.tiles[pt];
+        const TileDesc td = gw.tiles[gw.reverse ? gw.reverse - 1 - pt : pt];
         t.I = td.bi;
         t.J = td.bj;
         t.blk = gw.blocks[td.block];

@@ -109,7 +109,7 @@ struct TileInfo {
 __device__ __forceinline__ TileInfo tile_info(const GroupWork& gw, const EpiParams& ep, int t) {
     TileInfo ti;
     if (gw.tiles != nullptr) {
-        const TileDesc td = gw.tiles[t];
+        const TileDesc td = gw.tiles[gw.reverse ? gw.reverse - 1 - t : t];
         ti.bi = td.bi;
         ti.bj = td.bj;
         ti.blk = gw.blocks[td.block];

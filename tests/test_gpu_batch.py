@@ -261,3 +261,29 @@ def test_batch_pair_tiles_match_single_tiles(prec_name, sched_name):
             assert rp.rel_frobenius(y1, proj) <= 1e-4, n
             d = rp.rel_frobenius(y1, y0)
             assert d <= 5e-6, (n, d)
+
+
+def test_batch_serpentine_order_same_bits():
+    """Every other product walking its tile lists backwards changes the order
+    in which tiles run, not what any tile computes: the same bits, for both
+    tile shapes."""
+    import torch
+
+    from psd_projection_gb300.batch import BatchPlan, pack
+
+    sizes = [300, 40, 512, 129, 256, 90, 385]
+    mats = _blocks(sizes, seed=10)
+    pristine = pack(mats)
+    outs = []
+    with BatchPlan(sizes) as plan:
+        for pairs in (0, 1):
+            for serp in (0, 1):
+                plan.configure(pair_tiles=pairs, serpentine=serp)
+                assert plan.tuning()["serpentine"] == serp
+                d = pristine.clone()
+                plan.project(d)
+                torch.cuda.synchronize()
+                outs.append((pairs, serp, d.cpu().numpy()))
+    for pairs, serp, v in outs:
+        ref = next(w for p, s, w in outs if p == pairs and s == 0)
+        assert np.array_equal(v, ref), (pairs, serp)
