@@ -309,8 +309,9 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * before it left in L2.
  *
  * psdgb_batch_autotune times every tile shape, accumulator configuration,
- * tile order, serpentine order and (where available) the on-chip route on
- * the caller's scratch blocks (overwritten) and keeps the fastest.
+ * tile order and (where available) the on-chip route on the caller's scratch
+ * blocks (overwritten) and keeps the fastest; the serpentine order stays as
+ * configured (off by default).
  * psdgb_batch_configure sets them by hand (-1 keeps a setting; acc_mode
  * 0..2, tile_order 0 (largest blocks first) or 1 (block order),
  * small_on_chip, pair_tiles and serpentine 0 or 1 — small_on_chip or
