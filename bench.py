@@ -552,10 +552,6 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
         for pairs in (1, 0):
             routes["ms_pair_tiles" if pairs else "ms_single_tiles_only"] = timed(pair_tiles=pairs)
         plan.configure(pair_tiles=tuned["pair_tiles"])
-    if tuned["mid_blocks"] > 0:
-        for mid in (1, 0):
-            routes["ms_mid_one_cta" if mid else "ms_mid_grouped"] = timed(mid_one_cta=mid)
-        plan.configure(mid_one_cta=tuned["mid_one_cta"])
     work = pristine.clone()
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
@@ -613,8 +609,7 @@ def batched_session(count: int = 4096, seed: int = 0, replays: int = 5, evd_samp
             "autotune": {"best_ms": best, "acc_mode": info["acc_mode"], "tile_order": info["tile_order"],
                          "small_on_chip": tuned["small_on_chip"], "small_blocks": tuned["small_blocks"],
                          "pair_tiles": tuned["pair_tiles"], "num_pair_tiles": tuned["num_pair_tiles"],
-                         "serpentine": tuned["serpentine"], "mid_one_cta": tuned["mid_one_cta"],
-                         "mid_blocks": tuned["mid_blocks"],
+                         "serpentine": tuned["serpentine"],
                          "num_tiles": info["num_tiles"], "device_bytes": info["device_bytes"], **routes}}
 
 

@@ -304,27 +304,20 @@ psdgb_status psdgb_server_stats(psdgb_server* server, int* in_flight, int* queue
  * odd last tile row of a block stays on 128 x 128 tiles): half the operand
  * bytes per multiply-add.
  *
- * Blocks of 128 < n <= 256 (np = 256) with FP16 / FP16x3 operands can run
- * their whole chain with one CTA each instead (mid_one_cta = 1), a block's
- * three split matrices staying in L2 from one product to the next; the
- * result is the same bit for bit with one accumulator per tile (acc_mode 2).
- *
  * Serpentine order (serpentine = 1): every other product walks its tile lists
  * backwards, so that it starts on the blocks whose operands the product
  * before it left in L2.
  *
  * psdgb_batch_autotune times every tile shape, accumulator configuration,
  * tile order and (where available) the on-chip route on the caller's scratch
- * blocks (overwritten) and keeps the fastest (the one-CTA chain of the
- * blocks of np = 256 included); the serpentine order stays as configured
- * (off by default).
+ * blocks (overwritten) and keeps the fastest; the serpentine order stays as
+ * configured (off by default).
  * psdgb_batch_configure sets them by hand (-1 keeps a setting; acc_mode
  * 0..2, tile_order 0 (largest blocks first) or 1 (block order),
- * small_on_chip, pair_tiles, serpentine and mid_one_cta 0 or 1 —
- * small_on_chip, pair_tiles or mid_one_cta 1 is refused for plans without
- * such blocks); psdgb_batch_tuning reads them back, with the number of blocks
- * the on-chip route, of pair tiles the pair shape and of blocks the one-CTA
- * chain would take. */
+ * small_on_chip, pair_tiles and serpentine 0 or 1 — small_on_chip or
+ * pair_tiles 1 is refused for plans without such blocks); psdgb_batch_tuning
+ * reads them back, with the number of blocks the on-chip route and of pair
+ * tiles the pair shape would take. */
 typedef struct psdgb_batch psdgb_batch;
 psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precision, int schedule,
                                 psdgb_batch** out);
@@ -334,10 +327,9 @@ psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements,
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
 psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip,
-                                   int pair_tiles, int serpentine, int mid_one_cta);
+                                   int pair_tiles, int serpentine);
 psdgb_status psdgb_batch_tuning(const psdgb_batch* batch, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine,
-                                int* mid_one_cta, int64_t* mid_blocks);
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine);
 
 /* ---- eigenpairs and deflation ------------------------------------------------- */
 /* Replaces compute_eigenpairs (include/psd_projection/lanczos.h:19-44,

@@ -35,11 +35,11 @@ def _bind():
     lib.psdgb_batch_autotune.restype = c_int
     lib.psdgb_batch_autotune.argtypes = [vp, vp, vp, ctypes.POINTER(c_dbl)]
     lib.psdgb_batch_configure.restype = c_int
-    lib.psdgb_batch_configure.argtypes = [vp, c_int, c_int, c_int, c_int, c_int, c_int]
+    lib.psdgb_batch_configure.argtypes = [vp, c_int, c_int, c_int, c_int, c_int]
     lib.psdgb_batch_tuning.restype = c_int
     lib.psdgb_batch_tuning.argtypes = [vp, ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                        ctypes.POINTER(c_i64), ctypes.POINTER(c_int), ctypes.POINTER(c_i64),
-                                       ctypes.POINTER(c_int), ctypes.POINTER(c_int), ctypes.POINTER(c_i64)]
+                                       ctypes.POINTER(c_int)]
     _bound = True
     return lib
 
@@ -81,25 +81,21 @@ class BatchPlan:
                 "tile_order": to.value}
 
     def configure(self, acc_mode: int = -1, tile_order: int = -1, small_on_chip: int = -1,
-                  pair_tiles: int = -1, serpentine: int = -1, mid_one_cta: int = -1) -> None:
+                  pair_tiles: int = -1, serpentine: int = -1) -> None:
         """Set the accumulator mode (0..2), tile order (0 largest first, 1 block
         order), the on-chip route for blocks of n <= 128 (0 / 1), the 256 x 256
-        pair tiles for blocks of n > 128 (0 / 1), the serpentine product order
-        (0 / 1) and the one-CTA chain for blocks of 128 < n <= 256 (0 / 1);
-        -1 keeps."""
+        pair tiles for blocks of n > 128 (0 / 1) and the serpentine product
+        order (0 / 1); -1 keeps."""
         _capi.check(_bind().psdgb_batch_configure(self._h, acc_mode, tile_order, small_on_chip, pair_tiles,
-                                                  serpentine, mid_one_cta), "psdgb_batch_configure")
+                                                  serpentine), "psdgb_batch_configure")
 
     def tuning(self) -> dict:
         am, to, oc, sb, pt, npt, sp = c_int(), c_int(), c_int(), c_i64(), c_int(), c_i64(), c_int()
-        mo, mbk = c_int(), c_i64()
         _capi.check(_bind().psdgb_batch_tuning(self._h, ctypes.byref(am), ctypes.byref(to), ctypes.byref(oc),
                                                ctypes.byref(sb), ctypes.byref(pt), ctypes.byref(npt),
-                                               ctypes.byref(sp), ctypes.byref(mo), ctypes.byref(mbk)),
-                    "psdgb_batch_tuning")
+                                               ctypes.byref(sp)), "psdgb_batch_tuning")
         return {"acc_mode": am.value, "tile_order": to.value, "small_on_chip": oc.value, "small_blocks": sb.value,
-                "pair_tiles": pt.value, "num_pair_tiles": npt.value, "serpentine": sp.value,
-                "mid_one_cta": mo.value, "mid_blocks": mbk.value}
+                "pair_tiles": pt.value, "num_pair_tiles": npt.value, "serpentine": sp.value}
 
     def project(self, d_blocks, stream=None) -> None:
         import torch

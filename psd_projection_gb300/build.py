@@ -27,7 +27,7 @@ CFLAGS = [
     f"-I{ROOT / 'include'}", f"-I{CSRC}",
 ]
 SOURCES = ["capi.cu", "composite.cu", "elem.cu", "lanczos.cu", "gemm_simt.cu", "gemm_tc.cu", "gemm_tc2.cu", "gemm_wide.cu", "gemm_pairwide.cu", "eigenpairs.cu", "lobpcg.cu", "refapi.cu",
-           "static_scratch.cu", "serve.cu", "batch.cu", "batch_chain.cu", "batch_mid.cu"]
+           "static_scratch.cu", "serve.cu", "batch.cu", "batch_chain.cu"]
 
 
 def nvcc() -> str:

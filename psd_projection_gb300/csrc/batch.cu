@@ -439,20 +439,16 @@ struct psdgb_batch {
     size_t dev_bytes = 0;
     BlockDesc* blocks = nullptr;
     LzBlockDesc* lz = nullptr;
-    // Product tile lists.  t128[route][mid][shape][order]: the 128 x 128
-    // tiles (route 1 leaves out the blocks of np = 128, which run on chip;
-    // mid 1 the blocks of np = 256, which run one CTA each; shape 1 leaves to
-    // the pair tiles every pair of tile rows that lies inside a block of
-    // np >= 256, keeping the odd last tile row); tpair[mid][order]: those
+    // Product tile lists.  t128[route][shape][order]: the 128 x 128 tiles
+    // (route 1 leaves out the blocks of np = 128, which run on chip; shape 1
+    // leaves to the pair tiles every pair of tile rows that lies inside a
+    // block of np >= 256, keeping the odd last tile row); tpair[order]: those
     // 256 x 256 pair tiles (shape 1).  order 0: largest blocks first (LPT),
     // 1: block order.
-    TileDesc* t128[2][2][2][2] = {};
-    int64_t n128[2][2][2] = {};
-    TileDesc* tpair[2][2] = {};
-    int64_t npair[2] = {0, 0};
-    // The Xs split's blocks [route][mid] (null: every block).
-    int* xs_idx[2][2] = {};
-    int64_t xs_count[2][2] = {};
+    TileDesc* t128[2][2][2] = {};
+    int64_t n128[2][2] = {};
+    TileDesc* tpair[2] = {nullptr, nullptr};
+    int64_t npair = 0;
     BatchState* states = nullptr;
     float* a32 = nullptr;
     double* vec = nullptr;
@@ -470,14 +466,6 @@ struct psdgb_batch {
     int chain_count = 0;
     int* split_idx_big = nullptr;
     int64_t big_count = 0;
-    // Blocks of 128 < n <= 256 (np = 256) with FP16-pair operands can run
-    // their whole chain in one CTA each (batch_mid.cu), the grouped products
-    // leaving them out (t128[.][1]).
-    bool mid_ok = false;
-    ChainBlock* mid = nullptr;
-    int* mid_bidx = nullptr;
-    int mid_count = 0;
-    int use_mid = 0;
     // The small blocks' bound and chain run on a second stream (high
     // priority), forked from and joined back into the caller's stream.
     cudaStream_t side = nullptr;
@@ -558,22 +546,14 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
                                                           b->ld, split_idx);
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
-    const bool mid = b->use_mid && b->mid_ok;
-    if (mid) {
-        // the blocks of np = 256: their whole chain, one CTA each
-        const SplitMat mats[3] = {b->A, b->A2, b->A3};
-        PSDGB_TRY(launch_batch_mid(ds, b->precision, b->mid, b->mid_bidx, b->blocks, b->mid_count, mats, b->ld,
-                                   b->rows, coeffs, steps, d_blocks, 0, s));
-    }
     PrecisionInfo pi{};
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
     const int route = chain ? 1 : 0, shape = (b->shape && b->pairs_ok) ? 1 : 0;
-    const int mi = mid ? 1 : 0;
-    GroupWork gw{b->t128[route][mi][shape][b->order], b->blocks, 0};
-    const int64_t num_tiles = b->n128[route][mi][shape];
-    GroupWork gpw{b->tpair[mi][b->order], b->blocks, 0};
-    const int64_t num_pairs = shape ? b->npair[mi] : 0;
+    GroupWork gw{b->t128[route][shape][b->order], b->blocks, 0};
+    const int64_t num_tiles = b->n128[route][shape];
+    GroupWork gpw{b->tpair[b->order], b->blocks, 0};
+    const int64_t num_pairs = shape ? b->npair : 0;
     int nprod = 0;
     // One product over the big blocks: the pair tiles, then the 128 x 128
     // tiles (with the serpentine order, every other product the other way
@@ -628,13 +608,10 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         }
         PSDGB_TRY(product(b->A3, b->A2, e3));
     }
-    const int64_t xs_n = b->xs_count[route][mi];
-    if (xs_n > 0) {
-        batch_split_kernel<<<dim3(static_cast<unsigned>(xs_n), COPY_SPLIT), COPY_THREADS, 0, s>>>(
-            b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt, b->ld, b->xs_idx[route][mi]);  // Xs
-        count_launch();
-        PSDGB_CUDA_TRY(cudaGetLastError());
-    }
+    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt,
+                                                          b->ld, split_idx);  // Xs
+    count_launch();
+    PSDGB_CUDA_TRY(cudaGetLastError());
     EpiParams ef = base();
     ef.kind = EPI_FINAL;
     ef.dual = 1;
@@ -736,38 +713,28 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     // from it below).  Pair tiles (I, J), J <= I, cover tile rows 2I, 2I + 1
     // of blocks of np >= 256 up to the last even tile row.
     b->pairs_ok = pairwide_supported(precision);
-    const bool fp16_pairs = precision == PSDGB_PREC_FP16X3 || precision == PSDGB_PREC_FP16;
-    std::vector<int> mid_idx;  // blocks of np = 256 for the one-CTA chain
-    for (int64_t i = 0; i < count; ++i)
-        if (fp16_pairs && bd[i].np == 256) mid_idx.push_back(static_cast<int>(i));
-    b->mid_ok = !mid_idx.empty();
-    std::vector<TileDesc> l128[2][2][2], lpair[2];
+    std::vector<TileDesc> l128[2][2], lpair;
     for (int64_t i = 0; i < count; ++i) {
         const int nt = bd[i].np / 128;
-        const bool is_mid = b->mid_ok && bd[i].np == 256;
         const int full_rows = (nt >= 2 && b->pairs_ok) ? 2 * (nt / 2) : 0;  // tile rows on pair tiles (shape 1)
-        for (int mid = 0; mid < 2; ++mid) {
-            if (mid == 1 && is_mid) continue;  // one CTA each
-            for (int I = 0; I < full_rows / 2; ++I)
-                for (int J = 0; J <= I; ++J) lpair[mid].push_back(TileDesc{static_cast<int>(i), I, J, 0});
-            for (int route = 0; route < 2; ++route) {
-                if (route == 1 && nt == 1) continue;  // on chip
-                for (int shape = 0; shape < 2; ++shape)
-                    for (int bi = (shape ? full_rows : 0); bi < nt; ++bi)
-                        for (int bj = 0; bj <= bi; ++bj)
-                            l128[route][mid][shape].push_back(TileDesc{static_cast<int>(i), bi, bj, 0});
-            }
+        for (int I = 0; I < full_rows / 2; ++I)
+            for (int J = 0; J <= I; ++J) lpair.push_back(TileDesc{static_cast<int>(i), I, J, 0});
+        for (int route = 0; route < 2; ++route) {
+            if (route == 1 && nt == 1) continue;  // on chip
+            for (int shape = 0; shape < 2; ++shape)
+                for (int bi = (shape ? full_rows : 0); bi < nt; ++bi)
+                    for (int bj = 0; bj <= bi; ++bj) l128[route][shape].push_back(TileDesc{static_cast<int>(i), bi, bj, 0});
         }
     }
-    if (lpair[0].empty()) b->pairs_ok = false;
+    if (lpair.empty()) b->pairs_ok = false;
     b->shape = 0;  // 128 x 128 tiles until the autotuner or the caller picks pair tiles
     auto lpt = [&](std::vector<TileDesc> v) {
         std::stable_sort(v.begin(), v.end(),
                          [&](const TileDesc& a, const TileDesc& c) { return bd[a.block].np > bd[c.block].np; });
         return v;
     };
-    b->num_tiles = static_cast<int64_t>(l128[0][0][0].size());
-    for (int mid = 0; mid < 2; ++mid) b->npair[mid] = static_cast<int64_t>(lpair[mid].size());
+    b->num_tiles = static_cast<int64_t>(l128[0][0].size());
+    b->npair = static_cast<int64_t>(lpair.size());
     // Small blocks (one 128 x 128 tile, n >= 1) for the on-chip chain with
     // FP16-pair operands; the larger blocks' tile lists and split list.
     b->chain_ok = precision == PSDGB_PREC_FP16X3 || precision == PSDGB_PREC_FP16;
@@ -784,22 +751,6 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     b->chain_count = static_cast<int>(chain_idx.size());
     b->big_count = static_cast<int64_t>(big_idx.size());
     b->use_chain = b->chain_ok ? 1 : 0;
-    // the one-CTA chain takes its blocks largest first (block order otherwise)
-    std::stable_sort(mid_idx.begin(), mid_idx.end(), [&](int a, int c) { return b->n[a] > b->n[c]; });
-    b->mid_count = static_cast<int>(mid_idx.size());
-    b->use_mid = 0;
-    // The Xs split's block lists: every block (route 0) or the larger ones
-    // (route 1), without the one-CTA chain's blocks (mid 1).
-    std::vector<int> xs_list[2][2];
-    std::vector<char> is_big(static_cast<size_t>(count), 0);
-    for (int i : big_idx) is_big[static_cast<size_t>(i)] = 1;
-    for (int64_t i = 0; i < count; ++i)
-        for (int route = 0; route < 2; ++route)
-            for (int mid = 0; mid < 2; ++mid) {
-                const bool in_route = route == 0 || is_big[static_cast<size_t>(i)];
-                const bool is_mid = b->mid_ok && bd[i].np == 256;
-                if (in_route && !(mid == 1 && is_mid)) xs_list[route][mid].push_back(static_cast<int>(i));
-            }
     // Device memory: tables | states | FP32 copies | Lanczos vectors | operand planes.
     const size_t plane = static_cast<size_t>(b->rows) * b->ld * 2;
     const int nterms = format_terms(b->fmt);
@@ -807,10 +758,9 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_blocks = a256(sizeof(BlockDesc) * std::max<int64_t>(count, 1));
     const size_t sz_lz = a256(sizeof(LzBlockDesc) * std::max<int64_t>(count, 1));
     // every tile list, both orders, one after the other
-    size_t tile_entries = 2 * (lpair[0].size() + lpair[1].size());
+    size_t tile_entries = 2 * lpair.size();
     for (int r = 0; r < 2; ++r)
-        for (int m = 0; m < 2; ++m)
-            for (int sh = 0; sh < 2; ++sh) tile_entries += 2 * l128[r][m][sh].size();
+        for (int sh = 0; sh < 2; ++sh) tile_entries += 2 * l128[r][sh].size();
     const size_t sz_tiles = a256(sizeof(TileDesc) * std::max<size_t>(tile_entries, 1));
     const size_t sz_states = a256(sizeof(BatchState) * std::max<int64_t>(count, 1));
     const size_t sz_idx = a256(sizeof(int) * std::max<int64_t>(count, 1));
@@ -819,11 +769,8 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_ops = 3 * nterms * a256(plane);
     const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1)) + 256;
     const size_t sz_big_idx = a256(sizeof(int) * std::max<size_t>(big_idx.size(), 1));
-    const size_t sz_mid = a256(sizeof(ChainBlock) * std::max<size_t>(mid_idx.size(), 1)) +
-                          a256(sizeof(int) * std::max<size_t>(mid_idx.size(), 1));
-    const size_t sz_xs = 4 * a256(sizeof(int) * std::max<int64_t>(count, 1));
     b->dev_bytes = sz_blocks + sz_lz + sz_idx + sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain + sz_big_idx +
-                   sz_mid + sz_xs + sz_ops;
+                   sz_ops;
     cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -851,15 +798,6 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     p += sz_chain;
     b->split_idx_big = reinterpret_cast<int*>(p);
     p += sz_big_idx;
-    b->mid = reinterpret_cast<ChainBlock*>(p);
-    b->mid_bidx = reinterpret_cast<int*>(p + a256(sizeof(ChainBlock) * std::max<size_t>(mid_idx.size(), 1)));
-    p += sz_mid;
-    for (int r = 0; r < 2; ++r)
-        for (int m = 0; m < 2; ++m) {
-            b->xs_idx[r][m] = reinterpret_cast<int*>(p);
-            b->xs_count[r][m] = static_cast<int64_t>(xs_list[r][m].size());
-            p += a256(sizeof(int) * std::max<int64_t>(count, 1));
-        }
     SplitMat* mats[3] = {&b->A, &b->A2, &b->A3};
     for (int mi = 0; mi < 3; ++mi)
         for (int t = 0; t < 3; ++t) {
@@ -883,31 +821,17 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
             all.insert(all.end(), v.begin(), v.end());
         };
         for (int r = 0; r < 2; ++r)
-            for (int m = 0; m < 2; ++m)
-                for (int sh = 0; sh < 2; ++sh) {
-                    place(l128[r][m][sh], b->t128[r][m][sh]);
-                    b->n128[r][m][sh] = static_cast<int64_t>(l128[r][m][sh].size());
-                }
-        for (int m = 0; m < 2; ++m) place(lpair[m], b->tpair[m]);
+            for (int sh = 0; sh < 2; ++sh) {
+                place(l128[r][sh], b->t128[r][sh]);
+                b->n128[r][sh] = static_cast<int64_t>(l128[r][sh].size());
+            }
+        place(lpair, b->tpair);
         if (!all.empty())
             PSDGB_CUDA_TRY(cudaMemcpy(tile_store, all.data(), sizeof(TileDesc) * all.size(), cudaMemcpyHostToDevice));
     }
     if (!big_idx.empty())
         PSDGB_CUDA_TRY(cudaMemcpy(b->split_idx_big, big_idx.data(), sizeof(int) * big_idx.size(),
                                   cudaMemcpyHostToDevice));
-    for (int r = 0; r < 2; ++r)
-        for (int m = 0; m < 2; ++m)
-            if (!xs_list[r][m].empty())
-                PSDGB_CUDA_TRY(cudaMemcpy(b->xs_idx[r][m], xs_list[r][m].data(), sizeof(int) * xs_list[r][m].size(),
-                                          cudaMemcpyHostToDevice));
-    if (!mid_idx.empty()) {
-        std::vector<ChainBlock> mcb;
-        for (int i : mid_idx)
-            mcb.push_back(ChainBlock{b->a32 + lz[i].a32_off, lz[i].ld4, lz[i].n, lz[i].x_off, &b->states[i].scale,
-                                     &b->states[i].inv_scale});
-        PSDGB_CUDA_TRY(cudaMemcpy(b->mid, mcb.data(), sizeof(ChainBlock) * mcb.size(), cudaMemcpyHostToDevice));
-        PSDGB_CUDA_TRY(cudaMemcpy(b->mid_bidx, mid_idx.data(), sizeof(int) * mid_idx.size(), cudaMemcpyHostToDevice));
-    }
     if (b->chain_ok) {
         int least = 0, greatest = 0;
         PSDGB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
@@ -966,10 +890,9 @@ psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream)
 }
 
 psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip,
-                                   int pair_tiles, int serpentine, int mid_one_cta) {
+                                   int pair_tiles, int serpentine) {
     if (!b || acc_mode < -1 || acc_mode > ACC_1X4 || tile_order < -1 || tile_order > 1 || small_on_chip < -1 ||
-        small_on_chip > 1 || pair_tiles < -1 || pair_tiles > 1 || serpentine < -1 || serpentine > 1 ||
-        mid_one_cta < -1 || mid_one_cta > 1) {
+        small_on_chip > 1 || pair_tiles < -1 || pair_tiles > 1 || serpentine < -1 || serpentine > 1) {
         set_error("psdgb_batch_configure: bad arguments");
         return PSDGB_ERR_INVALID_ARGUMENT;
     }
@@ -984,19 +907,13 @@ psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order,
     if (acc_mode >= 0) b->acc_mode = acc_mode;
     if (tile_order >= 0) b->order = tile_order;
     if (small_on_chip >= 0) b->use_chain = small_on_chip;
-    if (mid_one_cta == 1 && !b->mid_ok) {
-        set_error("psdgb_batch_configure: no blocks of 128 < n <= 256 with FP16 / FP16x3 operands for one CTA each");
-        return PSDGB_ERR_INVALID_ARGUMENT;
-    }
     if (pair_tiles >= 0) b->shape = pair_tiles;
     if (serpentine >= 0) b->serpentine = serpentine;
-    if (mid_one_cta >= 0) b->use_mid = mid_one_cta;
     return PSDGB_OK;
 }
 
 psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_order, int* small_on_chip,
-                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine,
-                                int* mid_one_cta, int64_t* mid_blocks) {
+                                int64_t* small_blocks, int* pair_tiles, int64_t* num_pair_tiles, int* serpentine) {
     if (!b) {
         set_error("psdgb_batch_tuning: null batch");
         return PSDGB_ERR_INVALID_ARGUMENT;
@@ -1006,10 +923,8 @@ psdgb_status psdgb_batch_tuning(const psdgb_batch* b, int* acc_mode, int* tile_o
     if (small_on_chip) *small_on_chip = b->use_chain && b->chain_ok ? 1 : 0;
     if (small_blocks) *small_blocks = b->chain_ok ? b->chain_count : 0;
     if (pair_tiles) *pair_tiles = b->shape && b->pairs_ok ? 1 : 0;
-    if (num_pair_tiles) *num_pair_tiles = b->pairs_ok ? b->npair[0] : 0;
+    if (num_pair_tiles) *num_pair_tiles = b->pairs_ok ? b->npair : 0;
     if (serpentine) *serpentine = b->serpentine;
-    if (mid_one_cta) *mid_one_cta = b->use_mid && b->mid_ok ? 1 : 0;
-    if (mid_blocks) *mid_blocks = b->mid_ok ? b->mid_count : 0;
     return PSDGB_OK;
 }
 
@@ -1025,17 +940,16 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     PSDGB_CUDA_TRY(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_acc = b->acc_mode, best_order = b->order, best_chain = b->use_chain, best_shape = b->shape,
-        best_side = b->side_from, best_mid = b->use_mid;
+        best_side = b->side_from;
     const int accs[3] = {ACC_1X4, ACC_2X2, ACC_4X1};
-    // Every combination of: the one-CTA chain for the blocks of np = 256 (off,
-    // on), tile shape (128 x 128; pair tiles where available), small-block
-    // route (per product; on chip with the side stream taking the bound of
-    // n <= 128, or of n <= 256), accumulator configuration (3) and tile order
-    // (LPT, block order).  The serpentine order is left as configured (it
-    // measured no faster on the 4096-block configuration and would double
-    // the trials).
-    const int nsh = b->pairs_ok ? 2 : 1, nrt = b->chain_ok ? 3 : 1, nmid = b->mid_ok ? 2 : 1;
-    for (int cfg = 0; cfg < nmid * nsh * nrt * 3 * 2; ++cfg) {
+    // Every combination of: tile shape (128 x 128; pair tiles where
+    // available), small-block route (per product; on chip with the side
+    // stream taking the bound of n <= 128, or of n <= 256), accumulator
+    // configuration (3) and tile order (LPT, block order).  The serpentine
+    // order is left as configured (it measured no faster on the 4096-block
+    // configuration and would double the trials).
+    const int nsh = b->pairs_ok ? 2 : 1, nrt = b->chain_ok ? 3 : 1;
+    for (int cfg = 0; cfg < nsh * nrt * 3 * 2; ++cfg) {
         int c = cfg;
         const int o = c % 2;
         c /= 2;
@@ -1044,14 +958,11 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
         const int rt = c % nrt;
         c /= nrt;
         const int sh = c % nsh;
-        c /= nsh;
-        const int md = c;
         b->acc_mode = accs[ai];
         b->order = o;
         b->use_chain = rt > 0 ? 1 : 0;
         b->side_from = rt == 2 ? 1 : 2;
         b->shape = sh;
-        b->use_mid = md;
         PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));  // warm (and leaves valid operands)
         PSDGB_CUDA_TRY(cudaEventRecord(e0, s));
         PSDGB_TRY(batch_enqueue(b, d_scratch_blocks, s));
@@ -1066,7 +977,6 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
             best_chain = b->use_chain;
             best_side = b->side_from;
             best_shape = sh;
-            best_mid = md;
         }
     }
     b->acc_mode = best_acc;
@@ -1074,7 +984,6 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     b->use_chain = best_chain;
     b->side_from = best_side;
     b->shape = best_shape;
-    b->use_mid = best_mid;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms) *best_ms = best;

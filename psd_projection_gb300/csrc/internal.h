@@ -187,14 +187,6 @@ struct ChainBlock {
 psdgb_status launch_batch_chain(DeviceState* ds, int precision, const ChainBlock* d_blocks, int count,
                                 const float* coef, int steps, double* d_x, int* d_counter, int grid,
                                 cudaStream_t s);
-// The steps' products, the Xs split and the final product of `count` blocks
-// of np = 256 (FP16 / FP16x3), one CTA per block (batch_mid.cu): d_cb[i]
-// and d_blocks[d_bidx[i]] describe block i; mats are the A, A2, A3 split
-// matrices of the batch layout (row stride ld, `rows` rows), already holding
-// the first split.
-psdgb_status launch_batch_mid(DeviceState* ds, int precision, const ChainBlock* d_cb, const int* d_bidx,
-                              const BlockDesc* d_blocks, int count, const SplitMat (&mats)[3], int64_t ld,
-                              int64_t rows, const float* coef, int steps, double* d_x, int grid, cudaStream_t s);
 
 // ---- Lanczos (lanczos.cu) ---------------------------------------------------------
 struct LanczosResult {

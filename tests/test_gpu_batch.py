@@ -287,51 +287,3 @@ def test_batch_serpentine_order_same_bits():
     for pairs, serp, v in outs:
         ref = next(w for p, s, w in outs if p == pairs and s == 0)
         assert np.array_equal(v, ref), (pairs, serp)
-
-
-@pytest.mark.parametrize("prec_name,sched_name", [("fp16x3", "SCHEDULE_FP32"), ("fp16", "SCHEDULE_FP16")])
-def test_batch_mid_blocks_one_cta_bit_identical(prec_name, sched_name):
-    """The blocks of 128 < n <= 256 run their whole chain with one CTA each
-    (their split matrices staying in L2 between products) or on the grouped
-    products: the same tiles, sums and epilogue, so the same bits with one
-    accumulator per tile, with the small blocks on chip or not; each block
-    within 1e-4 (fp16x3) / 2e-3 (fp16) of FP64 EVD."""
-    import torch
-
-    import psd_projection_gb300 as psd
-    from psd_projection_gb300.batch import BatchPlan, pack, unpack
-
-    sizes = [129, 130, 192, 200, 255, 256, 40, 300, 512, 64, 170, 0, 1, 231]
-    mats = _blocks(sizes, seed=11)
-    pristine = pack(mats)
-    outs = {}
-    with BatchPlan(sizes, psd.PRECISIONS[prec_name], getattr(psd, sched_name)) as plan:
-        t = plan.tuning()
-        assert t["mid_blocks"] == sum(1 for n in sizes if 128 < n <= 256)
-        assert t["mid_one_cta"] == 0
-        for chip in (0, 1):
-            for mid in (1, 0):
-                plan.configure(acc_mode=2, small_on_chip=chip, mid_one_cta=mid)
-                assert plan.tuning()["mid_one_cta"] == mid
-                d = pristine.clone()
-                plan.project(d)
-                torch.cuda.synchronize()
-                outs[(chip, mid)] = d.cpu().numpy()
-    ref = outs[(0, 0)]
-    for key, v in outs.items():
-        assert np.array_equal(v, ref), key
-    tol = 1e-4 if prec_name == "fp16x3" else 2e-3
-    for n, x, y in zip(sizes, mats, unpack(torch.from_numpy(ref), sizes)):
-        if n >= 2:
-            proj, _ = rp.eig_psd(x)
-            assert rp.rel_frobenius(y, proj) <= tol, n
-
-
-def test_batch_mid_refused_without_fp16_pairs():
-    import psd_projection_gb300 as psd
-    from psd_projection_gb300.batch import BatchPlan
-
-    with BatchPlan([200, 64], psd.PRECISIONS["bf16x9"], psd.SCHEDULE_FP32) as plan:
-        assert plan.tuning()["mid_blocks"] == 0
-        with pytest.raises(psd.PsdgbError, match="one CTA each"):
-            plan.configure(mid_one_cta=1)
