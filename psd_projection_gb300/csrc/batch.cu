@@ -53,7 +53,6 @@ constexpr int LZ_CLASSES = 4;     // Lanczos CTA sizes 512, 256, 128, 64 threads
 // n threads, between 64 and 512.
 inline int lz_class(int64_t n) { return n > 256 ? 0 : (n > 128 ? 1 : (n > 64 ? 2 : 3)); }
 constexpr int COPY_THREADS = 256;  // 32 x 8 transpose tiles
-constexpr int COPY_SPLIT = 16;     // CTAs per block for the copy / split kernels
 
 struct BatchState {
     double theta, lo, up, scale, inv_scale;
@@ -343,85 +342,89 @@ __global__ void __launch_bounds__(T, 1024 / T) lz_batch_kernel(const LzBlockDesc
 }
 
 // The symmetric matrix defined by the upper triangle of column-major X_b,
-// written as FP32 rows (a32, n x ld4) — one CTA per block, 32x32 transposes.
-__global__ void batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs, const double* __restrict__ x,
-                                    float* a32) {
-    __shared__ float sm[32][33];
-    const LzBlockDesc d = descs[blockIdx.x];
-    if (d.n == 0) return;
-    const int n = d.n, ld4 = d.ld4;
-    const double* X = x + d.x_off;
-    float* A = a32 + d.a32_off;
-    const int tx = threadIdx.x % 32, ty0 = threadIdx.x / 32;
-    const int nt_r = (n + 31) / 32, nt_c = (ld4 + 31) / 32;
-    for (int t = blockIdx.y; t < nt_r * nt_c; t += gridDim.y) {
-        const int bi = t / nt_c, bj = t % nt_c;
+// written as FP32 rows (a32, n x ld4): one warp per 32 x 32 tile of the
+// batch's tile list (every block's tiles over rows < n, columns < ld4;
+// columns >= n written as zero), transposed through the warp's own
+// shared-memory tile, so no CTA idles on a small block and no CTA barrier
+// is needed.
+__global__ void __launch_bounds__(COPY_THREADS) batch_to_f32_kernel(const LzBlockDesc* __restrict__ descs,
+                                                                    const int4* __restrict__ tiles, int num_tiles,
+                                                                    const double* __restrict__ x, float* a32) {
+    __shared__ float sm[COPY_THREADS / 32][32][33];
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    float(&t)[32][33] = sm[warp];
+    for (int w = blockIdx.x * (COPY_THREADS / 32) + warp; w < num_tiles; w += gridDim.x * (COPY_THREADS / 32)) {
+        const int4 td = tiles[w];  // block, tile row, tile column
+        const LzBlockDesc d = descs[td.x];
+        const int n = d.n, ld4 = d.ld4, bi = td.y, bj = td.z;
+        const double* X = x + d.x_off;
+        float* A = a32 + d.a32_off;
         const int rbase = (bi <= bj) ? bi * 32 : bj * 32;
         const int cbase = (bi <= bj) ? bj * 32 : bi * 32;
-        __syncthreads();
-        for (int ty = ty0; ty < 32; ty += 8) {
-            const int r = rbase + tx, c = cbase + ty;
+        __syncwarp();
+#pragma unroll 8
+        for (int ty = 0; ty < 32; ++ty) {
+            const int r = rbase + lane, c = cbase + ty;
             // Narrowed on the integer ALUs (convert.h): FP64 issues slowly here.
-            sm[ty][tx] = (r < n && c < n) ? d2f_rn(X[r + static_cast<int64_t>(c) * n]) : 0.0f;
+            t[ty][lane] = (r < n && c < n) ? d2f_rn(X[r + static_cast<int64_t>(c) * n]) : 0.0f;
         }
-        __syncthreads();
-        for (int ty = ty0; ty < 32; ty += 8) {
-            const int i = bi * 32 + ty, j = bj * 32 + tx;
+        __syncwarp();
+#pragma unroll 8
+        for (int ty = 0; ty < 32; ++ty) {
+            const int i = bi * 32 + ty, j = bj * 32 + lane;
             if (i >= n || j >= ld4) continue;
-            float v = (bi < bj) ? sm[tx][ty] : (bi > bj) ? sm[ty][tx] : ((ty <= tx) ? sm[tx][ty] : sm[ty][tx]);
+            float v = (bi < bj) ? t[lane][ty] : (bi > bj) ? t[ty][lane] : ((ty <= lane) ? t[lane][ty] : t[ty][lane]);
             if (j >= n) v = 0.0f;
             A[static_cast<int64_t>(i) * ld4 + j] = v;
         }
     }
 }
 
-// Scaled operand terms of every block into the strided layout, from the
-// FP32 copy: the first split A = X / up, and again Xs = X / up for the final
+// Scaled operand terms of the blocks into the strided layout, from the FP32
+// copy: the first split A = X / up, and again Xs = X / up for the final
 // product (the copy holds exactly the FP32 narrowing of the symmetric matrix
-// X's upper triangle defines, which is what Xs needs).  The CTA walks the
-// 32 x 32 tiles of its block's np x np area (zero outside n), two at a time,
-// one per half; each thread writes 8 consecutive elements as one 16-byte
-// store per term plane.
+// X's upper triangle defines, which is what Xs needs).  One warp per 32 x 32
+// tile of the split's tile list (the tiles of each listed block that meet
+// its n x n corner; the rest of the block's np x np area is zero from the
+// plan's creation on and no product writes a nonzero there); lane l writes
+// columns 8 (l % 4) .. + 7 of rows l / 4 + 8 k as one 16-byte store per
+// term plane, 8 rows x 64 bytes per warp instruction.
 __global__ void __launch_bounds__(COPY_THREADS) batch_split_kernel(const LzBlockDesc* __restrict__ lz,
                                                                    const BlockDesc* __restrict__ blocks,
                                                                    const BatchState* __restrict__ states,
                                                                    const float* __restrict__ a32, SplitMat out,
                                                                    int fmt, int64_t ld,
-                                                                   const int* __restrict__ idx) {
-    static_assert(COPY_THREADS == 256, "two halves of 128 threads");
-    const int bidx = idx ? idx[blockIdx.x] : static_cast<int>(blockIdx.x);  // idx: a subset of the blocks
-    const LzBlockDesc d = lz[bidx];
-    const BlockDesc bd = blocks[bidx];
-    // The scaling runs in FP32, as in the single-matrix split.
-    const float inv = d2f_rn(states[bidx].inv_scale);
-    const int n = d.n, np = bd.np;
-    const int h = threadIdx.x / 128, ht = threadIdx.x % 128;
-    const int r = ht / 4, g = ht % 4;  // row r, columns 8g..8g+7 of the tile
-    const int nt = np / 32;
-    const int ntiles = nt * nt;
-    const float* A = a32 + d.a32_off;
-    const bool vec_ok = (d.ld4 % 4) == 0;
-    for (int tp = blockIdx.y; 2 * tp < ntiles; tp += gridDim.y) {
-        const int t = 2 * tp + h;
-        if (t >= ntiles) continue;
-        const int bi = t / nt, bj = t % nt;
-        const int i = bi * 32 + r, j0 = bj * 32 + 8 * g;
-        float v[8];
-        if (vec_ok && i < n && j0 + 8 <= n) {
-            const float* src = A + static_cast<int64_t>(i) * d.ld4 + j0;
-            const float4 u0 = *reinterpret_cast<const float4*>(src);
-            const float4 u1 = *reinterpret_cast<const float4*>(src + 4);
-            const float w[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+                                                                   const int4* __restrict__ tiles, int num_tiles) {
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int c8 = 8 * (lane & 3);
+    for (int w = blockIdx.x * (COPY_THREADS / 32) + warp; w < num_tiles; w += gridDim.x * (COPY_THREADS / 32)) {
+        const int4 td = tiles[w];  // block, tile row, tile column
+        const LzBlockDesc d = lz[td.x];
+        const BlockDesc bd = blocks[td.x];
+        // The scaling runs in FP32, as in the single-matrix split.
+        const float inv = d2f_rn(states[td.x].inv_scale);
+        const int n = d.n, j0 = td.z * 32 + c8;
+        const float* A = a32 + d.a32_off;
 #pragma unroll
-            for (int e = 0; e < 8; ++e) v[e] = w[e] * inv;
-        } else {
+        for (int k = 0; k < 4; ++k) {
+            const int i = td.y * 32 + (lane >> 2) + 8 * k;
+            float v[8];
+            if (i < n && j0 + 8 <= n) {  // ld4 is a multiple of 4: 16-byte rows
+                const float* src = A + static_cast<int64_t>(i) * d.ld4 + j0;
+                const float4 u0 = *reinterpret_cast<const float4*>(src);
+                const float4 u1 = *reinterpret_cast<const float4*>(src + 4);
+                const float w8[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                const float val = (i < n && j0 + e < n) ? A[static_cast<int64_t>(i) * d.ld4 + j0 + e] : 0.0f;
-                v[e] = val * inv;
+                for (int e = 0; e < 8; ++e) v[e] = w8[e] * inv;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const float val = (i < n && j0 + e < n) ? A[static_cast<int64_t>(i) * d.ld4 + j0 + e] : 0.0f;
+                    v[e] = val * inv;
+                }
             }
+            split_store8(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j0, v);
         }
-        split_store8(out, fmt, static_cast<size_t>(bd.row_base + i) * ld + bd.col_base + j0, v);
     }
 }
 
@@ -459,13 +462,20 @@ struct psdgb_batch {
     size_t lz_smem[LZ_CLASSES] = {0, 0, 0, 0};
     // Blocks of n <= 128 (one 128 x 128 tile) with FP16-pair operands can run
     // their whole chain on chip (batch_chain.cu); the grouped products then
-    // take only the larger blocks (t128[1], split_idx_big).
+    // take only the larger blocks (t128[1], split_tiles[1]).
     bool chain_ok = false;
     ChainBlock* chain = nullptr;
     int* chain_next = nullptr;  // the chain kernel's work counter
     int chain_count = 0;
-    int* split_idx_big = nullptr;
     int64_t big_count = 0;
+    // The splits' 32 x 32 tiles [route]: (block, tile row, tile column) for
+    // the tiles meeting each block's n x n corner, every block's (0) or the
+    // larger blocks' (1).
+    int4* split_tiles[2] = {nullptr, nullptr};
+    int64_t num_split_tiles[2] = {0, 0};
+    // The FP32 copy's 32 x 32 tiles (block, tile row, tile column).
+    int4* copy_tiles = nullptr;
+    int64_t num_copy_tiles = 0;
     // The small blocks' bound and chain run on a second stream (high
     // priority), forked from and joined back into the caller's stream.
     cudaStream_t side = nullptr;
@@ -491,9 +501,13 @@ namespace {
 psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
     DeviceState* ds = nullptr;
     PSDGB_TRY(device_state(&ds));
-    const int count = static_cast<int>(b->count);
-    const dim3 copy_grid(count, COPY_SPLIT);
-    batch_to_f32_kernel<<<copy_grid, COPY_THREADS, 0, s>>>(b->lz, d_blocks, b->a32);
+    if (b->num_copy_tiles > 0) {
+        const int64_t warps_needed = b->num_copy_tiles;
+        const int64_t ctas = std::min<int64_t>((warps_needed + COPY_THREADS / 32 - 1) / (COPY_THREADS / 32),
+                                               16 * static_cast<int64_t>(ds->sm_count));
+        batch_to_f32_kernel<<<static_cast<unsigned>(ctas), COPY_THREADS, 0, s>>>(
+            b->lz, b->copy_tiles, static_cast<int>(b->num_copy_tiles), d_blocks, b->a32);
+    }
     count_launch();
     PSDGB_CUDA_TRY(cudaGetLastError());
     // With the on-chip route, the blocks of n <= 128 (Lanczos classes 2 and
@@ -540,12 +554,17 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         // the larger blocks' bound of class 1 ran on the side stream
         if (b->side_from <= 1) PSDGB_CUDA_TRY(cudaStreamWaitEvent(s, b->ev_join, 0));
     }
-    const dim3 split_grid(static_cast<unsigned>(chain ? b->big_count : count), COPY_SPLIT);
-    const int* split_idx = chain ? b->split_idx_big : nullptr;
-    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A, b->fmt,
-                                                          b->ld, split_idx);
-    count_launch();
-    PSDGB_CUDA_TRY(cudaGetLastError());
+    // the split's tiles: every block's (route 0) or the larger blocks' (route 1)
+    const int4* split_tiles = b->split_tiles[chain ? 1 : 0];
+    const int64_t num_split = b->num_split_tiles[chain ? 1 : 0];
+    const unsigned split_ctas = static_cast<unsigned>(std::min<int64_t>(
+        (num_split + COPY_THREADS / 32 - 1) / (COPY_THREADS / 32), 16 * static_cast<int64_t>(ds->sm_count)));
+    if (num_split > 0) {
+        batch_split_kernel<<<split_ctas, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A, b->fmt,
+                                                               b->ld, split_tiles, static_cast<int>(num_split));
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
+    }
     PrecisionInfo pi{};
     precision_info(b->precision, &pi);
     const bool dual_step = pi.nprod == 1;
@@ -608,10 +627,12 @@ psdgb_status batch_enqueue(psdgb_batch* b, double* d_blocks, cudaStream_t s) {
         }
         PSDGB_TRY(product(b->A3, b->A2, e3));
     }
-    batch_split_kernel<<<split_grid, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt,
-                                                          b->ld, split_idx);  // Xs
-    count_launch();
-    PSDGB_CUDA_TRY(cudaGetLastError());
+    if (num_split > 0) {
+        batch_split_kernel<<<split_ctas, COPY_THREADS, 0, s>>>(b->lz, b->blocks, b->states, b->a32, b->A2, b->fmt,
+                                                               b->ld, split_tiles, static_cast<int>(num_split));  // Xs
+        count_launch();
+        PSDGB_CUDA_TRY(cudaGetLastError());
+    }
     EpiParams ef = base();
     ef.kind = EPI_FINAL;
     ef.dual = 1;
@@ -768,9 +789,34 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     const size_t sz_vec = a256(sizeof(double) * std::max<int64_t>(voff, 1));
     const size_t sz_ops = 3 * nterms * a256(plane);
     const size_t sz_chain = a256(sizeof(ChainBlock) * std::max<size_t>(chain_idx.size(), 1)) + 256;
-    const size_t sz_big_idx = a256(sizeof(int) * std::max<size_t>(big_idx.size(), 1));
+    std::vector<int4> split_list[2];
+    for (int route = 0; route < 2; ++route) {
+        auto add = [&](int64_t i) {
+            const int64_t nt = (b->n[i] + 31) / 32;
+            for (int64_t ti = 0; ti < nt; ++ti)
+                for (int64_t tj = 0; tj < nt; ++tj)
+                    split_list[route].push_back(make_int4(static_cast<int>(i), static_cast<int>(ti),
+                                                          static_cast<int>(tj), 0));
+        };
+        if (route == 0)
+            for (int64_t i = 0; i < count; ++i) add(i);
+        else
+            for (int i : big_idx) add(i);
+        b->num_split_tiles[route] = static_cast<int64_t>(split_list[route].size());
+    }
+    const size_t sz_big_idx = a256(sizeof(int4) * std::max<size_t>(split_list[0].size(), 1)) +
+                              a256(sizeof(int4) * std::max<size_t>(split_list[1].size(), 1));
+    std::vector<int4> copy_list;
+    for (int64_t i = 0; i < count; ++i) {
+        const int64_t n = b->n[i], ld4 = lz[i].ld4;
+        for (int64_t ti = 0; ti < (n + 31) / 32; ++ti)
+            for (int64_t tj = 0; tj < (ld4 + 31) / 32; ++tj)
+                copy_list.push_back(make_int4(static_cast<int>(i), static_cast<int>(ti), static_cast<int>(tj), 0));
+    }
+    b->num_copy_tiles = static_cast<int64_t>(copy_list.size());
+    const size_t sz_copy = a256(sizeof(int4) * std::max<size_t>(copy_list.size(), 1));
     b->dev_bytes = sz_blocks + sz_lz + sz_idx + sz_tiles + sz_states + sz_a32 + sz_vec + sz_chain + sz_big_idx +
-                   sz_ops;
+                   sz_copy + sz_ops;
     cudaError_t e = cudaMalloc(&b->dev, b->dev_bytes);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -796,8 +842,11 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     b->chain = reinterpret_cast<ChainBlock*>(p);
     b->chain_next = reinterpret_cast<int*>(p + sz_chain - 256);
     p += sz_chain;
-    b->split_idx_big = reinterpret_cast<int*>(p);
+    b->split_tiles[0] = reinterpret_cast<int4*>(p);
+    b->split_tiles[1] = reinterpret_cast<int4*>(p + a256(sizeof(int4) * std::max<size_t>(split_list[0].size(), 1)));
     p += sz_big_idx;
+    b->copy_tiles = reinterpret_cast<int4*>(p);
+    p += sz_copy;
     SplitMat* mats[3] = {&b->A, &b->A2, &b->A3};
     for (int mi = 0; mi < 3; ++mi)
         for (int t = 0; t < 3; ++t) {
@@ -829,8 +878,12 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         if (!all.empty())
             PSDGB_CUDA_TRY(cudaMemcpy(tile_store, all.data(), sizeof(TileDesc) * all.size(), cudaMemcpyHostToDevice));
     }
-    if (!big_idx.empty())
-        PSDGB_CUDA_TRY(cudaMemcpy(b->split_idx_big, big_idx.data(), sizeof(int) * big_idx.size(),
+    for (int route = 0; route < 2; ++route)
+        if (!split_list[route].empty())
+            PSDGB_CUDA_TRY(cudaMemcpy(b->split_tiles[route], split_list[route].data(),
+                                      sizeof(int4) * split_list[route].size(), cudaMemcpyHostToDevice));
+    if (!copy_list.empty())
+        PSDGB_CUDA_TRY(cudaMemcpy(b->copy_tiles, copy_list.data(), sizeof(int4) * copy_list.size(),
                                   cudaMemcpyHostToDevice));
     if (b->chain_ok) {
         int least = 0, greatest = 0;
