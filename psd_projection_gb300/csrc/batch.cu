@@ -20,9 +20,10 @@
 //                     larger blocks' bound
 //   batch_split       scaled operand terms of the larger blocks into one
 //                     strided layout
-//   3 x steps         per product: 256 x 256 pair tiles (gemm_pairwide.cu)
-//                     and grouped 128 x 128 tiles (gemm_tc.cu) over the tile
-//                     lists of the larger blocks
+//   3 x steps         per product: grouped 128 x 128 tiles (gemm_tc.cu) over
+//                     the tile list of the larger blocks, or also 256 x 256
+//                     pair tiles where a block's tile rows pair up
+//                     (gemm_pairwide.cu)
 //   batch_split (Xs)  Xs = X / up per block
 //   1 dual product    (X + up (Xs A + A Xs)/2) / 2 into the caller's blocks
 //
