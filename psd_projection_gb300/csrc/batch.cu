@@ -825,6 +825,13 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
         set_error("psdgb_batch_create: device allocation failed");
         return PSDGB_ERR_OUT_OF_MEMORY;
     }
+    // From here on a failing call frees the plan (memory, stream, events).
+    struct PlanGuard {
+        psdgb_batch* b;
+        ~PlanGuard() {
+            if (b) psdgb_batch_destroy(b);
+        }
+    } guard{b};
     char* p = static_cast<char*>(b->dev);
     b->blocks = reinterpret_cast<BlockDesc*>(p);
     p += sz_blocks;
@@ -908,6 +915,7 @@ psdgb_status psdgb_batch_create(const int64_t* sizes, int64_t count, int precisi
     if (b->lz_smem[0] > 48 * 1024)
         PSDGB_CUDA_TRY(cudaFuncSetAttribute(lz_batch_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             static_cast<int>(b->lz_smem[0])));
+    guard.b = nullptr;
     *out = b;
     return PSDGB_OK;
 }
