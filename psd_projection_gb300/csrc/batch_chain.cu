@@ -117,6 +117,7 @@ __device__ __forceinline__ void ldmatrix4(uint32_t addr, uint32_t (&r)[4]) {
 // (lane0 + 16 h + t / 4 + 8 rg, col + 8 cb + 2 (t % 4) + e) for thread t.
 __device__ __forceinline__ void tmem_ld_run(uint32_t taddr, float (&v)[2][16]) {
     uint32_t r[32];
+    __syncwarp();  // .sync.aligned: the whole warp, converged
     asm volatile(
         "tcgen05.ld.sync.aligned.16x256b.x4.b32 "
         "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%32];\n\t"
@@ -359,7 +360,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
             ch_mma<NPROD>(tmem, P, Q, dual, kbh);
             umma_commit(bar);
         }
-        if (!mbar_wait_bounded(bar, phase)) {
+        if (!mbar_wait_warp(bar, phase)) {  // warp-uniform: TMEM loads follow
             *abort_flag = 1;
             atomicCAS(cp.err, 0, DEVERR_EPI_WAIT);
         }
@@ -426,7 +427,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
             ch_epilogue(CH_STEP, sc, cp.coef[3 * s], cp.coef[3 * s + 1], cp.coef[3 * s + 2], mA, mA, mA3, dummy, tmem,
                         cb, nr, cp.x);
             operands_ready();
-            stop = *abort_flag != 0;
+            stop = __syncthreads_or(*abort_flag != 0) != 0;  // one answer for the whole CTA
         }
         if (stop) break;
         ch_split_from_f32(mA2, cb, inv);  // Xs
@@ -434,7 +435,7 @@ __global__ void __launch_bounds__(CH_THREADS, 1) batch_chain_kernel(const __grid
         product(sA2, sA, true);  // (Xs A + A Xs) / 2
         ch_epilogue(CH_FINAL, 0.5f * kF16AccUnscale, 0.f, 0.f, 0.f, nullptr, mA, mA3, dummy, tmem, cb, nr, cp.x);
         operands_ready();
-        stop = *abort_flag != 0;
+        stop = __syncthreads_or(*abort_flag != 0) != 0;
         if (threadIdx.x == 0) claim[0] = claim[1];
         __syncthreads();
     }

@@ -283,6 +283,18 @@ __device__ __forceinline__ bool mbar_wait_limit(uint64_t* bar, uint32_t parity, 
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
     return mbar_wait_limit(bar, parity, kWaitLimitNs);
 }
+// The same for all 32 lanes of a warp that goes on to warp-collective
+// (.sync.aligned) instructions such as tcgen05.ld: each lane polls on its own
+// and may leave its loop at another time, so the warp meets again here and
+// every lane gets the same outcome (false if any lane ran out of time).
+__device__ __forceinline__ bool mbar_wait_warp(uint64_t* bar, uint32_t parity) {
+    const bool ok = mbar_wait_bounded(bar, parity);
+    return __all_sync(0xffffffffu, ok);
+}
+// A flag read by every lane of a warp, with one answer for all of them.
+__device__ __forceinline__ bool warp_flag(const volatile int* flag) {
+    return __any_sync(0xffffffffu, *flag != 0);
+}
 
 // ---- TMA ------------------------------------------------------------------
 __device__ __forceinline__ void tma_load_2d(void* smem_dst, const void* tmap, uint64_t* bar, int x, int y) {
@@ -344,6 +356,7 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
 // Load 32 consecutive FP32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float (&v)[32]) {
     uint32_t r[32];
+    __syncwarp();  // .sync.aligned: the whole warp, converged
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
@@ -397,6 +410,11 @@ __device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t* bar, uint32_
         if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
     }
     return true;
+}
+// mbar_wait_cluster_bounded for a whole warp (see mbar_wait_warp).
+__device__ __forceinline__ bool mbar_wait_cluster_warp(uint64_t* bar, uint32_t parity) {
+    const bool ok = mbar_wait_cluster_bounded(bar, parity);
+    return __all_sync(0xffffffffu, ok);
 }
 // TMA load into this CTA's shared memory whose completion is counted on the
 // mbarrier at `bar_cluster_addr`, which may be in the peer CTA of the pair.

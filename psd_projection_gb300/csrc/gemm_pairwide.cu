@@ -256,12 +256,12 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PW_THREADS, 1)
             for (int c = 0; c < nchunks; ++c, ++gc) {
                 const int slot = gc & 1;
                 const uint32_t ph = static_cast<uint32_t>(gc >> 1) & 1u;
-                if (!mbar_wait_cluster_bounded(&acc_full[slot], ph)) {
+                if (!mbar_wait_cluster_warp(&acc_full[slot], ph)) {
                     record_error(err, abort_flag, DEVERR_EPI_WAIT);
                     stop = true;
                     break;
                 }
-                if (*abort_flag) {
+                if (warp_flag(abort_flag)) {
                     stop = true;
                     break;
                 }

@@ -207,11 +207,11 @@ __global__ void __launch_bounds__(64 + 32 * EW, 1)
             const int kb_total = tile_kblocks<KBE>(ep, ti) * dual_mult;
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
-            if (!mbar_wait_bounded(&acc_full[buf], use_ph)) {
+            if (!mbar_wait_warp(&acc_full[buf], use_ph)) {
                 record_error(err, abort_flag, DEVERR_EPI_WAIT);
                 break;
             }
-            if (*abort_flag) break;
+            if (warp_flag(abort_flag)) break;
             tc_fence_after();
             const int64_t p0 = ti.bi * BM + q4 * 32;
             const uint32_t tmem_row =

@@ -239,11 +239,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(THREADS, 1)
             pair_decode(pt, nt, group_rows, I, bj);
             const int buf = it % ACC_BUFS;
             const uint32_t use_ph = static_cast<uint32_t>(it / ACC_BUFS) & 1u;
-            if (!mbar_wait_cluster_bounded(&acc_full[buf], use_ph)) {
+            if (!mbar_wait_cluster_warp(&acc_full[buf], use_ph)) {
                 record_error(err, abort_flag, DEVERR_EPI_WAIT);
                 break;
             }
-            if (*abort_flag) break;
+            if (warp_flag(abort_flag)) break;
             tc_fence_after();
             const int64_t bi = 2 * I + rank;
             if (bi < nt) {

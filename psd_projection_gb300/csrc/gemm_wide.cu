@@ -277,12 +277,12 @@ __global__ void __launch_bounds__(W_THREADS, 1)
             for (int c = 0; c < nchunks; ++c, ++gc) {
                 const int slot = gc & 1;
                 const uint32_t ph = static_cast<uint32_t>(gc >> 1) & 1u;
-                if (!mbar_wait_bounded(&acc_full[slot], ph)) {
+                if (!mbar_wait_warp(&acc_full[slot], ph)) {
                     record_error(err, abort_flag, DEVERR_EPI_WAIT);
                     stop = true;
                     break;
                 }
-                if (*abort_flag) {
+                if (warp_flag(abort_flag)) {
                     stop = true;
                     break;
                 }
