@@ -325,6 +325,16 @@ psdgb_status psdgb_batch_destroy(psdgb_batch* batch);
 psdgb_status psdgb_batch_info(const psdgb_batch* batch, int64_t* total_elements, size_t* device_bytes,
                               int64_t* num_tiles, int* acc_mode, int* tile_order);
 psdgb_status psdgb_batch_project(psdgb_batch* batch, double* d_blocks, void* stream);
+/* The same projection as one CUDA graph launch: the plan captures its
+ * kernels once (for this d_blocks pointer and the current configuration; a
+ * new pointer, psdgb_batch_configure or psdgb_batch_autotune captures
+ * again) and instantiates the graph with the kernels' stream priorities
+ * kept, so that the small blocks' high-priority side stream overlaps the
+ * larger blocks' work as in psdgb_batch_project (a graph captured by the
+ * caller runs every kernel at the priority of the stream it is launched
+ * into).  The capture itself must not run inside the caller's own stream
+ * capture; later calls only launch the graph on stream. */
+psdgb_status psdgb_batch_project_graph(psdgb_batch* batch, double* d_blocks, void* stream);
 psdgb_status psdgb_batch_autotune(psdgb_batch* batch, double* d_scratch_blocks, void* stream, double* best_ms);
 psdgb_status psdgb_batch_configure(psdgb_batch* batch, int acc_mode, int tile_order, int small_on_chip,
                                    int pair_tiles, int serpentine);

@@ -32,6 +32,8 @@ def _bind():
                                      ctypes.POINTER(c_int), ctypes.POINTER(c_int)]
     lib.psdgb_batch_project.restype = c_int
     lib.psdgb_batch_project.argtypes = [vp, vp, vp]
+    lib.psdgb_batch_project_graph.restype = c_int
+    lib.psdgb_batch_project_graph.argtypes = [vp, vp, vp]
     lib.psdgb_batch_autotune.restype = c_int
     lib.psdgb_batch_autotune.argtypes = [vp, vp, vp, ctypes.POINTER(c_dbl)]
     lib.psdgb_batch_configure.restype = c_int
@@ -103,6 +105,16 @@ class BatchPlan:
         s = stream if stream is not None else torch.cuda.current_stream()
         _capi.check(_bind().psdgb_batch_project(self._h, ctypes.c_void_p(d_blocks.data_ptr()),
                                                 ctypes.c_void_p(s.cuda_stream)), "psdgb_batch_project")
+
+    def project_graph(self, d_blocks, stream=None) -> None:
+        """project() as one launch of a graph the plan captures once (per
+        d_blocks pointer and configuration) with the kernels' stream
+        priorities kept."""
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        _capi.check(_bind().psdgb_batch_project_graph(self._h, ctypes.c_void_p(d_blocks.data_ptr()),
+                                                      ctypes.c_void_p(s.cuda_stream)), "psdgb_batch_project_graph")
 
     def autotune(self, d_scratch, stream=None) -> float:
         import torch

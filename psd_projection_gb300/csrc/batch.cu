@@ -495,6 +495,14 @@ struct psdgb_batch {
     // starts on the blocks whose operands the product before left in L2.
     int serpentine = 0;
     bool pairs_ok = false;
+    // psdgb_batch_project_graph: the projection captured once on its own
+    // stream and instantiated with the kernels' stream priorities kept, for
+    // the blocks pointer and configuration it was captured with.
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    const double* g_blocks = nullptr;
+    bool g_stale = true;
+    uint64_t g_kernels = 0;  // kernels in the graph (counted again at each launch)
 };
 
 namespace {
@@ -927,6 +935,8 @@ psdgb_status psdgb_batch_destroy(psdgb_batch* b) {
     if (b->side) cudaStreamDestroy(b->side);
     if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->ev_join) cudaEventDestroy(b->ev_join);
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->cap) cudaStreamDestroy(b->cap);
     delete b;
     return PSDGB_OK;
 }
@@ -951,6 +961,49 @@ psdgb_status psdgb_batch_project(psdgb_batch* b, double* d_blocks, void* stream)
     return batch_enqueue(b, d_blocks, static_cast<cudaStream_t>(stream));
 }
 
+psdgb_status psdgb_batch_project_graph(psdgb_batch* b, double* d_blocks, void* stream) {
+    if (!b || (b->total_elems > 0 && !d_blocks)) {
+        set_error("psdgb_batch_project_graph: bad arguments");
+        return PSDGB_ERR_INVALID_ARGUMENT;
+    }
+    if (b->count == 0) return PSDGB_OK;
+    if (!b->gexec || b->g_stale || b->g_blocks != d_blocks) {
+        if (b->gexec) {
+            PSDGB_CUDA_TRY(cudaGraphExecDestroy(b->gexec));
+            b->gexec = nullptr;
+        }
+        if (!b->cap) PSDGB_CUDA_TRY(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking));
+        PSDGB_CUDA_TRY(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+        const uint64_t k0 = psdgb_kernel_launch_count();
+        const psdgb_status st = batch_enqueue(b, d_blocks, b->cap);
+        b->g_kernels = psdgb_kernel_launch_count() - k0;
+        count_launch(0 - b->g_kernels);  // captured, not run: counted at each launch below
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(b->cap, &g);  // always ends the capture
+        if (st != PSDGB_OK || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            if (st != PSDGB_OK) return st;
+            set_error(cudaGetErrorString(ce));
+            return PSDGB_ERR_CUDA;
+        }
+        // Node priorities: the small blocks' kernels keep the side stream's
+        // high priority inside the graph (by default a graph runs every
+        // kernel at the priority of the stream it is launched into).
+        const cudaError_t ie = cudaGraphInstantiateWithFlags(&b->gexec, g, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) {
+            b->gexec = nullptr;
+            set_error(cudaGetErrorString(ie));
+            return PSDGB_ERR_CUDA;
+        }
+        b->g_blocks = d_blocks;
+        b->g_stale = false;
+    }
+    PSDGB_CUDA_TRY(cudaGraphLaunch(b->gexec, static_cast<cudaStream_t>(stream)));
+    count_launch(b->g_kernels);
+    return PSDGB_OK;
+}
+
 psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order, int small_on_chip,
                                    int pair_tiles, int serpentine) {
     if (!b || acc_mode < -1 || acc_mode > ACC_1X4 || tile_order < -1 || tile_order > 1 || small_on_chip < -1 ||
@@ -971,6 +1024,7 @@ psdgb_status psdgb_batch_configure(psdgb_batch* b, int acc_mode, int tile_order,
     if (small_on_chip >= 0) b->use_chain = small_on_chip;
     if (pair_tiles >= 0) b->shape = pair_tiles;
     if (serpentine >= 0) b->serpentine = serpentine;
+    b->g_stale = true;
     return PSDGB_OK;
 }
 
@@ -1046,6 +1100,7 @@ psdgb_status psdgb_batch_autotune(psdgb_batch* b, double* d_scratch_blocks, void
     b->use_chain = best_chain;
     b->side_from = best_side;
     b->shape = best_shape;
+    b->g_stale = true;
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (best_ms) *best_ms = best;

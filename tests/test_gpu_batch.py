@@ -287,3 +287,40 @@ def test_batch_serpentine_order_same_bits():
     for pairs, serp, v in outs:
         ref = next(w for p, s, w in outs if p == pairs and s == 0)
         assert np.array_equal(v, ref), (pairs, serp)
+
+
+def test_batch_plan_graph_same_bits():
+    """psdgb_batch_project_graph (the plan's own graph, stream priorities
+    kept) reproduces psdgb_batch_project bit for bit: on first capture, on
+    replay, after a configuration change and for another blocks pointer."""
+    import torch
+
+    from psd_projection_gb300.batch import BatchPlan, pack
+
+    sizes = [300, 40, 512, 129, 256, 90, 385, 16]
+    mats = _blocks(sizes, seed=13)
+    pristine = pack(mats)
+    with BatchPlan(sizes) as plan:
+        ref = pristine.clone()
+        plan.project(ref)
+        torch.cuda.synchronize()
+        ref = ref.cpu().numpy()
+        d = pristine.clone()
+        for _ in range(3):  # capture, then two replays on restored input
+            d.copy_(pristine)
+            plan.project_graph(d)
+            torch.cuda.synchronize()
+            assert np.array_equal(d.cpu().numpy(), ref)
+        other = pristine.clone()  # a new pointer: captured again
+        plan.project_graph(other)
+        torch.cuda.synchronize()
+        assert np.array_equal(other.cpu().numpy(), ref)
+        for chip in (0, 1):  # a new configuration: captured again, same bits (acc_mode 2)
+            plan.configure(acc_mode=2, small_on_chip=chip)
+            d.copy_(pristine)
+            plan.project_graph(d)
+            torch.cuda.synchronize()
+            r = pristine.clone()
+            plan.project(r)
+            torch.cuda.synchronize()
+            assert np.array_equal(d.cpu().numpy(), r.cpu().numpy()), chip
