@@ -129,6 +129,22 @@ def test_unknown_method_is_rejected_before_any_device_work(lib):
     assert st == 1
 
 
+def test_batch_entry_points_reject_a_null_plan(lib):
+    """The batch plan's entry points check their arguments before any device
+    work (host logic only)."""
+    import ctypes
+
+    vp = ctypes.c_void_p
+    for name in ("psdgb_batch_project", "psdgb_batch_project_graph"):
+        fn = getattr(lib, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = [vp, vp, vp]
+        assert fn(None, None, None) == 1, name  # PSDGB_ERR_INVALID_ARGUMENT
+    lib.psdgb_batch_destroy.restype = ctypes.c_int
+    lib.psdgb_batch_destroy.argtypes = [vp]
+    assert lib.psdgb_batch_destroy(None) == 0
+
+
 def test_version(lib):
     assert lib.psdgb_version() >= 10000
     assert lib.psdgb_kernel_launch_count() == 0 or lib.psdgb_kernel_launch_count() > 0
